@@ -1,0 +1,93 @@
+"""Pin the CPU oracle against the reference's own C++ outputs.
+
+tests/golden/reference_vectors.json was produced by tests/golden/make_golden.py
+from the reference host headers (p20_exact_math.hpp, coarse_exact_core.hpp,
+p19_monster_gate.hpp). Every comparison is bit-exact.
+"""
+import ctypes
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_vectors.json")))
+
+
+def _f(h):
+    return np.array([int(h, 16)], np.uint64).view(np.float64)[0]
+
+
+def _bits(a):
+    return [format(int(v), "016x") for v in np.asarray(a, np.float64).view(np.uint64)]
+
+
+def test_world_states_match_reference():
+    for rec in GOLDEN["world_states"]:
+        perm, abc = po.world_state(rec["seed"], rec["index"])
+        assert hashlib.sha256(perm.tobytes() + abc.tobytes()).hexdigest() == rec["sha256"], rec
+        assert _bits(abc) == rec["abc"]
+
+
+def test_octave_columns_match_reference():
+    L = po.lib()
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    for rec in GOLDEN["columns"]:
+        perm, abc = po.world_state(rec["seed"], rec["index"])
+        x, z, sy = _f(rec["x"]), _f(rec["z"]), _f(rec["sy"])
+        full = np.zeros(17)
+        L.or_perlin_column17_test(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, 0, P(full, ctypes.c_double))
+        assert _bits(full) == rec["full17"]
+        up = np.zeros(17)
+        L.or_perlin_column17_test(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, 11, P(up, ctypes.c_double))
+        assert _bits(up[11:]) == rec["upper6"]
+
+
+def test_p19_scores_match_reference():
+    L = po.lib()
+    for rec in GOLDEN["p19"]:
+        f = po.Features(*rec["features"])
+        s = L.or_p19_score(rec["scout"], ctypes.byref(f))
+        assert _bits([s])[0] == rec["score"], rec
+        assert L.or_p19_extreme(ctypes.byref(f)) == rec["extreme"]
+
+
+def test_coarse_signs_and_scores_match_reference():
+    for rec in GOLDEN["coarse"]:
+        sg = po.coarse_signs(rec["seed"])
+        assert hashlib.sha256(sg.tobytes()).hexdigest() == rec["signs_sha256"]
+        assert po.coarse_score(rec["seed"]) == rec["score"]
+
+
+def test_splitmix_matches_reference():
+    for rec in GOLDEN["splitmix"]:
+        assert po.splitmix_seed(rec["sequence"], rec["attempt"]) == int(rec["seed"])
+
+
+@pytest.mark.skipif(po.ref() is None and not os.path.isdir("/root/reference"), reason="reference checkout absent")
+def test_oracle_against_live_reference_random():
+    """Extra random cases straight against the reference harness when it is built here."""
+    R = po.ref() or (po.build_ref() and po.ref())
+    if R is None:
+        pytest.skip("reference harness not buildable")
+    L = po.lib()
+    P = lambda a, t: a.ctypes.data_as(ctypes.POINTER(t))
+    rng = np.random.default_rng(99)
+    for _ in range(500):
+        seed = int(rng.integers(-2**63, 2**63 - 1))
+        idx = int(rng.integers(0, 76))
+        perm, abc = po.world_state(seed, idx)
+        rp = np.zeros(256, np.uint8)
+        ra = np.zeros(3)
+        R.ref_world_state(seed, idx, P(rp, ctypes.c_uint8), P(ra, ctypes.c_double))
+        assert np.array_equal(perm, rp) and _bits(abc) == _bits(ra)
+        x, z = rng.uniform(-1e5, 1e5, 2)
+        sy = float(rng.uniform(0.01, 700))
+        a = np.zeros(17)
+        b = np.zeros(17)
+        L.or_perlin_column17_test(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, 0, P(a, ctypes.c_double))
+        R.ref_perlin3_full17(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, P(b, ctypes.c_double))
+        assert _bits(a) == _bits(b)
