@@ -1,0 +1,308 @@
+"""BetaSeedFinder GB300: Python host mirror of the worker's C ABI (include/bsf.h).
+
+The compute path is libbsf.so (hand-written sm_103a CUDA kernels). This module
+only loads it with ctypes and mirrors the reference's caller-facing interface:
+`GpuStage0Scout` / `GpuP20Scout` batch filters (src/GpuStage0Scout.java,
+src/GpuP20Scout.java), the exact chunk terrain of `BetaTerrain173`, the exact
+island scan and preview of `IslandSearchEngine`, and the batch MEGA search.
+There is no CPU fallback: if the extension is missing or no GPU is usable the
+calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbsf.so")
+WORKER_PATH = os.path.join(HERE, "_build", "bsf_worker")
+
+PROFILE_GENERAL, PROFILE_MEGA, PROFILE_RECORD60, PROFILE_RECORD80 = 0, 1, 2, 3
+PROFILES = {"general": 0, "mega": 1, "record60": 2, "record80": 3}
+MODE_QUEUED, MODE_PLAIN = 0, 1
+CENTER_CHUNK_X = (0, 15, 0, 15, -15, -15, 0, 15)
+CENTER_CHUNK_Z = (0, 0, 15, 15, 0, 15, -15, -15)
+
+
+class BsfError(RuntimeError):
+    pass
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("capacity", ctypes.c_uint32), ("profile", ctypes.c_int32),
+                ("research", ctypes.c_int32), ("centers", ctypes.c_int32), ("max_exact_radius", ctypes.c_int32)]
+
+
+class MatchSettings(ctypes.Structure):
+    _fields_ = [("min_blocks", ctypes.c_int32), ("min_columns", ctypes.c_int32),
+                ("min_y_for_match", ctypes.c_int32), ("min_width", ctypes.c_int32),
+                ("min_depth", ctypes.c_int32), ("min_avg_thickness", ctypes.c_double)]
+
+
+class Island(ctypes.Structure):
+    _fields_ = [("found", ctypes.c_int32), ("blocks", ctypes.c_int32), ("columns", ctypes.c_int32),
+                ("min_x", ctypes.c_int32), ("max_x", ctypes.c_int32), ("min_z", ctypes.c_int32),
+                ("max_z", ctypes.c_int32), ("min_y", ctypes.c_int32), ("max_y", ctypes.c_int32),
+                ("center_x", ctypes.c_int32), ("center_z", ctypes.c_int32),
+                ("touches_side", ctypes.c_int32), ("touches_bottom", ctypes.c_int32),
+                ("radius_used", ctypes.c_int32), ("sum_x", ctypes.c_int64), ("sum_z", ctypes.c_int64)]
+
+    def key(self):
+        return (self.found, self.blocks, self.columns, self.min_x, self.max_x, self.min_z, self.max_z,
+                self.min_y, self.max_y, self.center_x, self.center_z, self.touches_side, self.radius_used)
+
+
+class MegaRecord(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_int64), ("world_index", ctypes.c_int32), ("center_index", ctypes.c_int32),
+                ("center_chunk_x", ctypes.c_int32), ("center_chunk_z", ctypes.c_int32),
+                ("p20", ctypes.c_int32), ("upper", ctypes.c_int32), ("high", ctypes.c_int32),
+                ("coarse", ctypes.c_int32), ("p19_score", ctypes.c_double), ("island", Island)]
+
+
+class StageCounts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "worlds", "regions", "p20_passed", "upper_passed", "high_passed", "p19_passed",
+        "mega_rejected", "coarse_evaluated", "coarse_passed", "islands", "rng_fallbacks")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
+           "bsf_set_mode", "bsf_stage0_filter", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
+           "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
+           "bsf_kernel_launches"]
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libbsf.so (build it with betaseedfinder_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise BsfError("libbsf.so not built at %s; run betaseedfinder_gb300.build.build()" % path)
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    vp, i64p, u8p, u64p, i32p = ctypes.c_void_p, P(ctypes.c_int64), P(ctypes.c_uint8), P(ctypes.c_uint64), P(ctypes.c_int32)
+    L.bsf_default_config.argtypes = [P(Config)]
+    L.bsf_default_match_settings.argtypes = [P(MatchSettings)]
+    L.bsf_open.argtypes = [P(Config)]
+    L.bsf_open.restype = vp
+    L.bsf_close.argtypes = [vp]
+    L.bsf_last_error.argtypes = [vp]
+    L.bsf_last_error.restype = ctypes.c_char_p
+    L.bsf_set_mode.argtypes = [vp, ctypes.c_int32]
+    L.bsf_stage0_filter.argtypes = [vp, i64p, ctypes.c_uint32, u8p, ctypes.c_size_t]
+    L.bsf_p20_filter.argtypes = [vp, i64p, ctypes.c_uint32, u8p, ctypes.c_size_t]
+    L.bsf_chunk_bitmaps.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, u8p, u64p]
+    L.bsf_exact_scan.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                 P(MatchSettings), P(Island)]
+    L.bsf_resolve_region.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                     ctypes.c_int32, P(MatchSettings), P(Island)]
+    L.bsf_preview.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                              P(MatchSettings), P(Island), i32p, i32p, ctypes.c_uint32]
+    L.bsf_mega_search.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, P(MatchSettings), P(MegaRecord),
+                                  ctypes.c_uint32, P(ctypes.c_uint32), P(StageCounts)]
+    L.bsf_mega_search_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, P(MatchSettings),
+                                         P(MegaRecord), ctypes.c_uint32, P(ctypes.c_uint32), P(StageCounts),
+                                         ctypes.c_void_p]
+    L.bsf_kernel_launches.argtypes = [vp]
+    L.bsf_kernel_launches.restype = ctypes.c_uint64
+    _lib = L
+    return L
+
+
+def default_match_settings(**overrides):
+    s = MatchSettings()
+    load().bsf_default_match_settings(ctypes.byref(s))
+    for k, v in overrides.items():
+        setattr(s, k, v)
+    return s
+
+
+def _p(a, t):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+class Worker:
+    """One GPU worker handle (the C ABI's bsf_handle)."""
+
+    def __init__(self, capacity=32768, profile=PROFILE_MEGA, research=False, centers=8, max_exact_radius=24,
+                 device=0):
+        L = load()
+        cfg = Config()
+        L.bsf_default_config(ctypes.byref(cfg))
+        cfg.device, cfg.capacity = device, capacity
+        cfg.profile = PROFILES.get(profile, profile) if isinstance(profile, str) else profile
+        cfg.research, cfg.centers, cfg.max_exact_radius = int(research), centers, max_exact_radius
+        self.cfg = cfg
+        self._h = L.bsf_open(ctypes.byref(cfg))
+        if not self._h:
+            raise BsfError("bsf_open failed")
+        err = L.bsf_last_error(self._h)
+        if err:
+            msg = err.decode()
+            L.bsf_close(self._h)
+            self._h = None
+            raise BsfError("bsf_open: " + msg)
+
+    def close(self):
+        if self._h:
+            load().bsf_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, status):
+        if status != 0:
+            raise BsfError("status %d: %s" % (status, load().bsf_last_error(self._h).decode()))
+
+    @property
+    def record_bytes(self):
+        return 34 if self.cfg.research else 16
+
+    @property
+    def kernel_launches(self):
+        return int(load().bsf_kernel_launches(self._h))
+
+    def set_mode(self, mode):
+        self._check(load().bsf_set_mode(self._h, mode))
+
+    def stage0_filter(self, seeds):
+        """stage0stream response body: count * centers records (numpy uint8)."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        out = np.zeros(len(seeds) * self.cfg.centers * self.record_bytes, np.uint8)
+        self._check(load().bsf_stage0_filter(self._h, _p(seeds, ctypes.c_int64), len(seeds),
+                                             _p(out, ctypes.c_uint8), out.nbytes))
+        return out
+
+    def p20_filter(self, seeds):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        out = np.zeros(len(seeds), np.uint8)
+        self._check(load().bsf_p20_filter(self._h, _p(seeds, ctypes.c_int64), len(seeds),
+                                          _p(out, ctypes.c_uint8), out.nbytes))
+        return out
+
+    def chunk_bitmaps(self, seeds, chunk_x=0, chunk_z=0):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        bm = np.zeros((len(seeds), 4096), np.uint8)
+        h = np.zeros(len(seeds), np.uint64)
+        self._check(load().bsf_chunk_bitmaps(self._h, _p(seeds, ctypes.c_int64), len(seeds), chunk_x, chunk_z,
+                                             _p(bm, ctypes.c_uint8), _p(h, ctypes.c_uint64)))
+        return bm, h
+
+    def exact_scan(self, seed, center_chunk_x=0, center_chunk_z=0, radius=7, settings=None):
+        out = Island()
+        s = settings or default_match_settings()
+        self._check(load().bsf_exact_scan(self._h, seed, center_chunk_x, center_chunk_z, radius, ctypes.byref(s),
+                                          ctypes.byref(out)))
+        return out
+
+    def resolve_region(self, seed, center_chunk_x, center_chunk_z, radius, coarse, settings=None):
+        out = Island()
+        s = settings or default_match_settings()
+        self._check(load().bsf_resolve_region(self._h, seed, center_chunk_x, center_chunk_z, radius, coarse,
+                                              ctypes.byref(s), ctypes.byref(out)))
+        return out
+
+    def preview(self, seed, center_chunk_x=0, center_chunk_z=0, radius=7, settings=None, capacity=1 << 20):
+        out = Island()
+        s = settings or default_match_settings()
+        mn = np.zeros(capacity, np.int32)
+        mx = np.zeros(capacity, np.int32)
+        self._check(load().bsf_preview(self._h, seed, center_chunk_x, center_chunk_z, radius, ctypes.byref(s),
+                                       ctypes.byref(out), _p(mn, ctypes.c_int32), _p(mx, ctypes.c_int32), capacity))
+        if not out.found:
+            return out, None, None
+        n = (out.max_x - out.min_x + 1) * (out.max_z - out.min_z + 1)
+        return out, mn[:n].copy(), mx[:n].copy()
+
+    def mega_search(self, seeds, radius=7, settings=None, records_cap=4096):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        s = settings or default_match_settings()
+        recs = (MegaRecord * records_cap)()
+        n = ctypes.c_uint32(0)
+        counts = StageCounts()
+        self._check(load().bsf_mega_search(self._h, _p(seeds, ctypes.c_int64), len(seeds), radius, ctypes.byref(s),
+                                           recs, records_cap, ctypes.byref(n), ctypes.byref(counts)))
+        return counts, [recs[i] for i in range(n.value)]
+
+    def mega_search_device(self, d_seeds_ptr, count, radius=7, settings=None, records_cap=4096, stream=None):
+        s = settings or default_match_settings()
+        recs = (MegaRecord * records_cap)()
+        n = ctypes.c_uint32(0)
+        counts = StageCounts()
+        self._check(load().bsf_mega_search_device(self._h, ctypes.c_void_p(d_seeds_ptr), count, radius,
+                                                  ctypes.byref(s), recs, records_cap, ctypes.byref(n),
+                                                  ctypes.byref(counts), ctypes.c_void_p(stream or 0)))
+        return counts, [recs[i] for i in range(n.value)]
+
+
+class GpuStage0Scout:
+    """Mirror of src/GpuStage0Scout.java: filter(seeds, count) -> BatchResult arrays."""
+
+    def __init__(self, capacity=32768, profile="general", research=True, centers=8):
+        self.worker = Worker(capacity=capacity, profile=profile, research=research, centers=centers,
+                             max_exact_radius=1)
+        self.centers = centers
+
+    def center_count(self):
+        return self.centers
+
+    def center_chunk_x(self, i):
+        return CENTER_CHUNK_X[i]
+
+    def center_chunk_z(self, i):
+        return CENTER_CHUNK_Z[i]
+
+    def result_index(self, world_index, center_index):
+        return world_index * self.centers + center_index
+
+    def filter(self, seeds, count=None):
+        seeds = np.asarray(seeds, dtype=np.int64)[: (len(seeds) if count is None else count)]
+        raw = self.worker.stage0_filter(seeds)
+        return decode_records(raw, self.worker.record_bytes)
+
+    def close(self):
+        self.worker.close()
+
+
+def decode_records(raw, record_bytes):
+    """Decode stage0stream records into the Java BatchResult field arrays (GpuStage0Scout.java:290-335)."""
+    r = np.asarray(raw, np.uint8).reshape(-1, record_bytes)
+    u16 = lambda o: r[:, o].astype(np.int32) | (r[:, o + 1].astype(np.int32) << 8)
+    out = {
+        "p20Counts": r[:, 0].copy(), "fullUpperCounts": r[:, 1].copy(), "highReentryCounts": r[:, 2].copy(),
+        "p19Pass": r[:, 3].copy(), "coarseScores": u16(4), "p19ExtremeBypass": r[:, 6].copy(),
+        "megaTopologyRejected": r[:, 7].copy(),
+        "p19Scores": np.ascontiguousarray(r[:, 8:16]).view(np.float64).ravel(),
+    }
+    if record_bytes == 34:
+        out.update({"p19FullY88": u16(16), "p19FullY96": u16(18), "p19FullY104": u16(20), "p19FullY112": u16(22),
+                    "p19Y88LargestCluster": u16(24), "p19Y88Width": r[:, 26].copy(), "p19Y88Depth": r[:, 27].copy(),
+                    "p19Y88TouchesBorder": r[:, 28].copy(), "p19Y96LargestCluster": u16(29),
+                    "p19Y96Width": r[:, 31].copy(), "p19Y96Depth": r[:, 32].copy(),
+                    "p19Y96TouchesBorder": r[:, 33].copy()})
+    return out
+
+
+def splitmix_seed(sequence_seed, attempt):
+    """deterministicSeedForAttempt (src/IslandSearchEngine.java:2551-2556), as a signed int64."""
+    m = (1 << 64) - 1
+    z = (sequence_seed + attempt * 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    z ^= z >> 31
+    return z - (1 << 64) if z >= 1 << 63 else z

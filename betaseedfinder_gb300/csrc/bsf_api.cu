@@ -1,0 +1,644 @@
+// Host side of libbsf: the C ABI of include/bsf.h, device buffer ownership and
+// the two batch pipeline forms (queued and plain stage-by-stage).
+#include "../../include/bsf.h"
+#include "bsf_device.cuh"
+#include "bsf_internal.h"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace bsf {
+namespace {
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        char buf[320];
+        std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+        throw std::runtime_error(buf);
+    }
+}
+
+// Response record packing (gpu_p20_benchmark.cpp:7504-7554): lean 16 bytes or
+// research 34 bytes per region, world-major / centre-minor.
+__global__ void k_pack_records(const RegionInfo* __restrict__ regions, int count, int research,
+                               std::uint8_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const RegionInfo r = regions[i];
+    const int rec = research ? 34 : 16;
+    std::uint8_t* o = out + static_cast<std::size_t>(i) * rec;
+    auto clamp8 = [](int v) { return static_cast<std::uint8_t>(v < 0 ? 0 : (v > 255 ? 255 : v)); };
+    o[0] = clamp8(r.p20);
+    o[1] = clamp8(r.upper);
+    o[2] = clamp8(r.high);
+    o[3] = r.p19Pass;
+    o[4] = static_cast<std::uint8_t>(r.coarse & 0xFF);
+    o[5] = static_cast<std::uint8_t>((r.coarse >> 8) & 0xFF);
+    o[6] = r.p19Extreme;
+    o[7] = r.megaReject;
+    const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(r.p19Score));
+    for (int k = 0; k < 8; ++k) o[8 + k] = static_cast<std::uint8_t>(bits >> (8 * k));
+    if (!research) return;
+    auto put16 = [&](int off, int v) {
+        const unsigned u = static_cast<unsigned>(v < 0 ? 0 : (v > 65535 ? 65535 : v));
+        o[off] = static_cast<std::uint8_t>(u & 0xFF);
+        o[off + 1] = static_cast<std::uint8_t>((u >> 8) & 0xFF);
+    };
+    put16(16, r.fullY88);
+    put16(18, r.fullY96);
+    put16(20, r.fullY104);
+    put16(22, r.fullY112);
+    put16(24, r.y88Largest);
+    o[26] = r.y88Width;
+    o[27] = r.y88Depth;
+    o[28] = r.y88Touches ? 1 : 0;
+    put16(29, r.y96Largest);
+    o[31] = r.y96Width;
+    o[32] = r.y96Depth;
+    o[33] = r.y96Touches ? 1 : 0;
+}
+
+// P20-only response byte (gpu_p20_benchmark.cpp:7660-7668).
+__global__ void k_pack_p20(const RegionInfo* __restrict__ regions, int count, int centers, std::uint8_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int v = regions[static_cast<std::size_t>(i) * centers].p20;
+    out[i] = static_cast<std::uint8_t>(v < 0 ? 0 : (v > 255 ? 255 : v));
+}
+
+// Stage pass counters (gpu_p20_benchmark.cpp:7556-7571) and the exact-stage queue.
+__global__ void k_stage_counts(const RegionInfo* __restrict__ regions, int count, Profile prof,
+                               unsigned long long* counts, RegionRef* exactQueue, int* exactCount, int exactCap,
+                               int centers) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (i < count) {
+        const RegionInfo r = regions[i];
+        const bool p20 = r.p20 >= prof.p20MinCount;
+        const bool up = p20 && r.upper >= prof.upperMinCount;
+        const bool hi = up && r.high >= prof.highMinCount;
+        c[0] = p20;
+        c[1] = up;
+        c[2] = hi;
+        c[3] = hi && r.p19Pass;
+        c[4] = hi && r.p19Pass && r.megaReject;
+        c[5] = r.coarseEvaluated;
+        c[6] = r.coarseEvaluated && r.coarse >= prof.coarseMinCells;
+        if (c[6]) {
+            const int slot = atomicAdd(exactCount, 1);
+            if (slot < exactCap) exactQueue[slot] = RegionRef{i / centers, i % centers};
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        unsigned long long v = c[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&counts[k], v);
+    }
+}
+
+}  // namespace
+}  // namespace bsf
+
+using namespace bsf;
+
+struct BsfHandle {
+    bsf_config cfg{};
+    Profile prof{};
+    int mode = BSF_MODE_QUEUED;
+    bool ok = false;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    unsigned long long launches = 0;
+    int capacity = 0;
+    int centers = 8;
+    int coarseCap = 0;
+    int exactCap = 0;
+
+    std::int64_t* dSeeds = nullptr;
+    StateCache cache;
+    RegionInfo* dRegions = nullptr;
+    RegionRef* dCoarseQueue = nullptr;
+    int* dCounters = nullptr;  // [0] coarse count, [1] rng fallbacks, [2] exact count
+    std::uint32_t* dSigns = nullptr;
+    int* dLabels = nullptr;
+    int* dStats = nullptr;
+    std::uint8_t* dOut = nullptr;
+    std::uint64_t* dHashes = nullptr;
+    unsigned long long* dStageCounts = nullptr;
+    RegionRef* dExactQueue = nullptr;
+    void* dExactBase = nullptr;
+    ExactScratch exact;
+    Island* dIsland = nullptr;
+    int* dPrevMin = nullptr;
+    int* dPrevMax = nullptr;
+    int prevCap = 0;
+    std::int64_t* hSeeds = nullptr;  // pinned staging
+    std::uint8_t* hOut = nullptr;
+    std::size_t outBytes = 0;
+    std::vector<RegionInfo> hRegions;
+
+    void alloc(void** p, std::size_t bytes, const char* what) { check(cudaMalloc(p, bytes), what); }
+};
+
+namespace {
+
+void fail(BsfHandle* h, const std::string& msg) {
+    if (h) h->err = msg;
+}
+
+template <typename F>
+int guarded(void* hv, F&& f) {
+    BsfHandle* h = static_cast<BsfHandle*>(hv);
+    if (!h) return BSF_E_ARG;
+    if (!h->ok) {
+        if (h->err.empty()) h->err = "handle is not open";
+        return BSF_E_STATE;
+    }
+    try {
+        return f(h);
+    } catch (const std::invalid_argument& e) {
+        fail(h, e.what());
+        return BSF_E_ARG;
+    } catch (const std::length_error& e) {
+        fail(h, e.what());
+        return BSF_E_LIMIT;
+    } catch (const std::exception& e) {
+        fail(h, e.what());
+        const cudaError_t sticky = cudaGetLastError();
+        if (sticky != cudaSuccess) h->ok = false;
+        return BSF_E_CUDA;
+    }
+}
+
+MatchSettings to_ms(const bsf_match_settings* s) {
+    bsf_match_settings d;
+    if (!s) {
+        bsf_default_match_settings(&d);
+        s = &d;
+    }
+    return MatchSettings{s->min_blocks, s->min_columns, s->min_y_for_match, s->min_width, s->min_depth,
+                         s->min_avg_thickness};
+}
+
+void to_island(const Island& i, bsf_island* o) {
+    o->found = i.found;
+    o->blocks = i.blocks;
+    o->columns = i.columns;
+    o->min_x = i.minX; o->max_x = i.maxX; o->min_z = i.minZ; o->max_z = i.maxZ;
+    o->min_y = i.minY; o->max_y = i.maxY;
+    o->center_x = i.centerX; o->center_z = i.centerZ;
+    o->touches_side = i.touchesSide; o->touches_bottom = i.touchesBottom;
+    o->radius_used = i.radiusUsed;
+    o->sum_x = i.sumX; o->sum_z = i.sumZ;
+}
+
+// H2D seeds and build every generator of the batch.
+void stage_seeds(BsfHandle* h, const std::int64_t* seeds, int n, bool hostSeeds) {
+    if (hostSeeds) {
+        std::memcpy(h->hSeeds, seeds, static_cast<std::size_t>(n) * 8);
+        check(cudaMemcpyAsync(h->dSeeds, h->hSeeds, static_cast<std::size_t>(n) * 8, cudaMemcpyHostToDevice, h->stream),
+              "seed upload");
+        launch_world_init(h->dSeeds, n, h->cache, h->dCounters + 1, h->stream);
+    } else {
+        launch_world_init(seeds, n, h->cache, h->dCounters + 1, h->stream);
+    }
+    ++h->launches;
+}
+
+// Queued form: fused Stage0 kernel appends P19 survivors to the device coarse
+// queue; the coarse kernels consume it by its device-side count.
+void run_gpu_stages_queued(BsfHandle* h, int n) {
+    check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
+    launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, h->dCoarseQueue, h->dCounters,
+                  h->capacity * h->centers, h->stream);
+    launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, LatticeBuffers{}, h->dSigns,
+                        h->dLabels, h->dStats, h->dRegions, h->centers, h->stream);
+    h->launches += 3;
+}
+
+// Plain form: stage by stage with a host round trip after each; the host
+// rebuilds the coarse work list and feeds it in micro-batches of 1024 regions
+// (the reference worker's structure, gpu_p20_benchmark.cpp:7421-7502, 1188-1218).
+void run_gpu_stages_plain(BsfHandle* h, int n) {
+    check(cudaStreamSynchronize(h->stream), "world init");
+    launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, nullptr, h->dCounters, 0, h->stream);
+    ++h->launches;
+    const int regions = n * h->centers;
+    h->hRegions.resize(regions);
+    check(cudaMemcpyAsync(h->hRegions.data(), h->dRegions, sizeof(RegionInfo) * regions, cudaMemcpyDeviceToHost,
+                          h->stream),
+          "region download");
+    check(cudaStreamSynchronize(h->stream), "stage0");
+    std::vector<RegionRef> list;
+    for (int i = 0; i < regions; ++i) {
+        const RegionInfo& r = h->hRegions[i];
+        if (r.p19Evaluated && r.p19Pass && !r.megaReject) list.push_back(RegionRef{i / h->centers, i % h->centers});
+    }
+    const int micro = std::min(1024, h->coarseCap);
+    for (std::size_t off = 0; off < list.size(); off += micro) {
+        const int chunk = static_cast<int>(std::min<std::size_t>(micro, list.size() - off));
+        check(cudaMemcpyAsync(h->dCoarseQueue, list.data() + off, sizeof(RegionRef) * chunk, cudaMemcpyHostToDevice,
+                              h->stream),
+              "coarse list upload");
+        check(cudaMemcpyAsync(h->dCounters, &chunk, sizeof(int), cudaMemcpyHostToDevice, h->stream), "count");
+        launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, chunk, LatticeBuffers{}, h->dSigns, h->dLabels,
+                            h->dStats, h->dRegions, h->centers, h->stream);
+        h->launches += 2;
+        check(cudaStreamSynchronize(h->stream), "coarse micro-batch");
+    }
+}
+
+void run_gpu_stages(BsfHandle* h, int n) {
+    if (h->mode == BSF_MODE_PLAIN) run_gpu_stages_plain(h, n);
+    else run_gpu_stages_queued(h, n);
+}
+
+Island exact_once(BsfHandle* h, int world, int ccx, int ccz, int radius, const MatchSettings& ms, bool preview) {
+    if (radius > h->exact.maxRadius) throw std::length_error("exact radius exceeds the provisioned max_exact_radius");
+    launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, h->exact, h->dIsland, preview ? h->dPrevMin : nullptr,
+                      preview ? h->dPrevMax : nullptr, h->prevCap, false, h->stream);
+    h->launches += 12;
+    Island isl;
+    check(cudaMemcpyAsync(&isl, h->dIsland, sizeof(Island), cudaMemcpyDeviceToHost, h->stream), "island download");
+    check(cudaStreamSynchronize(h->stream), "exact scan");
+    int err = 0;
+    check(cudaMemcpy(&err, h->exact.err, sizeof(int), cudaMemcpyDeviceToHost), "err");
+    if (err) throw std::runtime_error("exact scan union-find exceeded its retry bound");
+    return isl;
+}
+
+int compare_island(const Island& a, const Island& b) {
+    if (a.blocks != b.blocks) return a.blocks < b.blocks ? -1 : 1;
+    if (a.columns != b.columns) return a.columns < b.columns ? -1 : 1;
+    const int areaA = (a.maxX - a.minX + 1) * (a.maxZ - a.minZ + 1);
+    const int areaB = (b.maxX - b.minX + 1) * (b.maxZ - b.minZ + 1);
+    if (areaA != areaB) return areaA < areaB ? -1 : 1;
+    return 0;
+}
+
+// verifySideBorderMatch (IslandSearchEngine.java:3188-3260).
+bool border_verify(BsfHandle* h, int world, int ccx, int ccz, const MatchSettings& ms, Island& best) {
+    static const int radii[5] = {10, 13, 16, 20, 24};
+    for (int r : radii) {
+        if (r <= best.radiusUsed) continue;
+        const Island e = exact_once(h, world, ccx, ccz, r, ms, false);
+        if (!e.found) return false;
+        best = e;
+        if (!best.touchesSide) return true;
+    }
+    return true;
+}
+
+// processGpuRegionAttempt (IslandSearchEngine.java:1878-1971).
+Island resolve(BsfHandle* h, int world, int ccx, int ccz, int radius, int coarse, const MatchSettings& ms) {
+    Island normal = exact_once(h, world, ccx, ccz, radius, ms, false);
+    bool have = normal.found != 0;
+    if (have && normal.touchesSide && radius < 24) have = border_verify(h, world, ccx, ccz, ms, normal);
+    Island match = normal;
+    if (radius < 16 && coarse >= 120) {
+        Island hot = exact_once(h, world, ccx, ccz, 16, ms, false);
+        bool haveHot = hot.found != 0;
+        if (haveHot && hot.touchesSide && hot.radiusUsed < 24) haveHot = border_verify(h, world, ccx, ccz, ms, hot);
+        if (haveHot && (!have || compare_island(hot, match) > 0)) {
+            match = hot;
+            have = true;
+        }
+    }
+    if (!have) {
+        Island none{};
+        none.radiusUsed = radius;
+        return none;
+    }
+    return match;
+}
+
+int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, uint32_t count,
+               int32_t radius, const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
+               uint32_t* recordsCount, bsf_stage_counts* counts) {
+    if (!seeds || count == 0 || count > static_cast<uint32_t>(h->capacity) || (!records && recordsCap))
+        throw std::invalid_argument("bsf_mega_search: bad seeds/count/records");
+    if (radius < 0 || radius > h->exact.maxRadius) throw std::length_error("radius exceeds max_exact_radius");
+    const MatchSettings ms = to_ms(s);
+    cudaStream_t saved = h->stream;
+    if (userStream) h->stream = userStream;
+    const int n = static_cast<int>(count);
+    check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
+    check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
+    stage_seeds(h, seeds, n, hostSeeds);
+    run_gpu_stages(h, n);
+    const int regions = n * h->centers;
+    k_stage_counts<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, h->prof, h->dStageCounts,
+                                                                h->dExactQueue, h->dCounters + 2, h->exactCap,
+                                                                h->centers);
+    ++h->launches;
+    check(cudaGetLastError(), "k_stage_counts");
+    unsigned long long hc[8];
+    int hcount[4];
+    check(cudaMemcpyAsync(hc, h->dStageCounts, sizeof(hc), cudaMemcpyDeviceToHost, h->stream), "counts");
+    check(cudaMemcpyAsync(hcount, h->dCounters, sizeof(hcount), cudaMemcpyDeviceToHost, h->stream), "counts");
+    check(cudaStreamSynchronize(h->stream), "mega batch");
+    if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
+    const int exactN = std::min(hcount[2], h->exactCap);
+    std::vector<RegionRef> ex(exactN);
+    std::vector<RegionInfo> info(exactN);
+    if (exactN) {
+        check(cudaMemcpy(ex.data(), h->dExactQueue, sizeof(RegionRef) * exactN, cudaMemcpyDeviceToHost), "exact list");
+        std::sort(ex.begin(), ex.end(), [](const RegionRef& a, const RegionRef& b) {
+            return a.world != b.world ? a.world < b.world : a.center < b.center;
+        });
+        for (int k = 0; k < exactN; ++k)
+            check(cudaMemcpy(&info[k], h->dRegions + static_cast<std::size_t>(ex[k].world) * h->centers + ex[k].center,
+                             sizeof(RegionInfo), cudaMemcpyDeviceToHost),
+                  "region info");
+    }
+    unsigned long long islands = 0;
+    uint32_t written = 0;
+    for (int k = 0; k < exactN; ++k) {
+        const int ccx = center_chunk_x(ex[k].center), ccz = center_chunk_z(ex[k].center);
+        const Island isl = resolve(h, ex[k].world, ccx, ccz, radius, info[k].coarse, ms);
+        if (isl.found) ++islands;
+        if (written < recordsCap) {
+            bsf_mega_record& r = records[written++];
+            std::int64_t seed = 0;
+            if (hostSeeds) seed = seeds[ex[k].world];
+            else check(cudaMemcpy(&seed, seeds + ex[k].world, 8, cudaMemcpyDeviceToHost), "seed");
+            r.seed = seed;
+            r.world_index = ex[k].world;
+            r.center_index = ex[k].center;
+            r.center_chunk_x = ccx;
+            r.center_chunk_z = ccz;
+            r.p20 = info[k].p20;
+            r.upper = info[k].upper;
+            r.high = info[k].high;
+            r.coarse = info[k].coarse;
+            r.p19_score = info[k].p19Score;
+            to_island(isl, &r.island);
+        }
+    }
+    if (recordsCount) *recordsCount = written;
+    if (counts) {
+        counts->worlds = count;
+        counts->regions = static_cast<uint64_t>(regions);
+        counts->p20_passed = hc[0];
+        counts->upper_passed = hc[1];
+        counts->high_passed = hc[2];
+        counts->p19_passed = hc[3];
+        counts->mega_rejected = hc[4];
+        counts->coarse_evaluated = hc[5];
+        counts->coarse_passed = hc[6];
+        counts->islands = islands;
+        counts->rng_fallbacks = static_cast<uint64_t>(hcount[1]);
+    }
+    h->stream = saved;
+    return BSF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void bsf_default_config(bsf_config* c) {
+    if (!c) return;
+    c->device = 0;
+    c->capacity = 32768;
+    c->profile = BSF_PROFILE_MEGA;
+    c->research = 0;
+    c->centers = 8;
+    c->max_exact_radius = 24;
+}
+
+void bsf_default_match_settings(bsf_match_settings* s) {
+    if (!s) return;
+    s->min_blocks = 1000;
+    s->min_columns = 100;
+    s->min_y_for_match = 60;
+    s->min_width = 10;
+    s->min_depth = 10;
+    s->min_avg_thickness = 2.0;
+}
+
+void* bsf_open(const bsf_config* cfgIn) {
+    BsfHandle* h = new (std::nothrow) BsfHandle();
+    if (!h) return nullptr;
+    bsf_config cfg;
+    bsf_default_config(&cfg);
+    if (cfgIn) cfg = *cfgIn;
+    h->cfg = cfg;
+    try {
+        if (cfg.capacity < 1 || cfg.capacity > (1u << 22)) throw std::invalid_argument("capacity must be 1..4194304");
+        if (cfg.centers != 1 && cfg.centers != 8) throw std::invalid_argument("centers must be 1 or 8");
+        if (cfg.profile < 0 || cfg.profile > 3) throw std::invalid_argument("profile must be 0..3");
+        if (cfg.max_exact_radius < 1 || cfg.max_exact_radius > 24)
+            throw std::invalid_argument("max_exact_radius must be 1..24");
+        check(cudaSetDevice(cfg.device), "cudaSetDevice");
+        check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+        init_lcg_tables();
+        h->capacity = static_cast<int>(cfg.capacity);
+        h->centers = cfg.centers;
+        h->prof = profile_by_id(cfg.profile);
+        const std::size_t n = static_cast<std::size_t>(h->capacity);
+        const std::size_t regions = n * h->centers;
+        h->coarseCap = static_cast<int>(std::min<std::size_t>(regions, 1u << 14));
+        h->exactCap = 4096;
+        h->alloc(reinterpret_cast<void**>(&h->dSeeds), n * 8, "seeds");
+        h->alloc(reinterpret_cast<void**>(&h->cache.perms), n * WORLD_PERM_BYTES, "state cache");
+        h->alloc(reinterpret_cast<void**>(&h->cache.offsets), n * WORLD_OFFSETS * 8, "state cache");
+        h->cache.capacity = h->capacity;
+        h->alloc(reinterpret_cast<void**>(&h->dRegions), regions * sizeof(RegionInfo), "regions");
+        h->alloc(reinterpret_cast<void**>(&h->dCoarseQueue), regions * sizeof(RegionRef), "coarse queue");
+        h->alloc(reinterpret_cast<void**>(&h->dCounters), 16 * sizeof(int), "counters");
+        const std::size_t cc = static_cast<std::size_t>(h->coarseCap);
+        h->alloc(reinterpret_cast<void**>(&h->dSigns), cc * 61 * 61 * 4, "coarse signs");
+        const std::size_t ctas = static_cast<std::size_t>(coarse_score_ctas());
+        h->alloc(reinterpret_cast<void**>(&h->dLabels), ctas * 61 * 61 * 17 * 4, "coarse labels");
+        h->alloc(reinterpret_cast<void**>(&h->dStats), ctas * 61 * 61 * 17 * 8 + 64, "coarse stats");
+        h->outBytes = regions * (cfg.research ? 34 : 16) + 64;
+        h->alloc(reinterpret_cast<void**>(&h->dOut), std::max<std::size_t>(h->outBytes, n * 4096), "output");
+        h->alloc(reinterpret_cast<void**>(&h->dHashes), n * 8, "hashes");
+        h->alloc(reinterpret_cast<void**>(&h->dStageCounts), 8 * sizeof(unsigned long long), "stage counts");
+        h->alloc(reinterpret_cast<void**>(&h->dExactQueue), h->exactCap * sizeof(RegionRef), "exact queue");
+        const std::size_t eb = exact_scratch_bytes(cfg.max_exact_radius);
+        h->alloc(&h->dExactBase, eb, "exact scratch");
+        exact_scratch_carve(h->exact, h->dExactBase, cfg.max_exact_radius);
+        check(cudaMemset(h->exact.err, 0, 64), "memset");
+        h->alloc(reinterpret_cast<void**>(&h->dIsland), sizeof(Island), "island");
+        h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
+        h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+        h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hSeeds), n * 8), "pinned seeds");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
+              "pinned output");
+        check(cudaDeviceSynchronize(), "open");
+        h->ok = true;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        h->ok = false;
+    }
+    return h;
+}
+
+void bsf_close(void* hv) {
+    BsfHandle* h = static_cast<BsfHandle*>(hv);
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void* dev[] = {h->dSeeds, h->cache.perms, h->cache.offsets, h->dRegions, h->dCoarseQueue, h->dCounters,
+                   h->dSigns, h->dLabels, h->dStats, h->dOut, h->dHashes, h->dStageCounts, h->dExactQueue,
+                   h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    if (h->hSeeds) cudaFreeHost(h->hSeeds);
+    if (h->hOut) cudaFreeHost(h->hOut);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+const char* bsf_last_error(const void* hv) {
+    const BsfHandle* h = static_cast<const BsfHandle*>(hv);
+    if (!h) return "null handle";
+    return h->err.c_str();
+}
+
+int bsf_set_mode(void* hv, int32_t mode) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (mode != BSF_MODE_QUEUED && mode != BSF_MODE_PLAIN) throw std::invalid_argument("mode must be 0 or 1");
+        h->mode = mode;
+        return BSF_OK;
+    });
+}
+
+int bsf_stage0_filter(void* hv, const int64_t* seeds, uint32_t count, uint8_t* out, size_t outLen) {
+    return guarded(hv, [&](BsfHandle* h) {
+        const std::size_t rec = h->cfg.research ? 34 : 16;
+        if (!seeds || !out || count == 0 || count > static_cast<uint32_t>(h->capacity))
+            throw std::invalid_argument("bsf_stage0_filter: bad seeds/out/count (count must be 1..capacity)");
+        const std::size_t need = static_cast<std::size_t>(count) * h->centers * rec;
+        if (outLen < need) throw std::invalid_argument("bsf_stage0_filter: out_len too small");
+        const int n = static_cast<int>(count);
+        check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
+        stage_seeds(h, seeds, n, true);
+        run_gpu_stages(h, n);
+        const int regions = n * h->centers;
+        k_pack_records<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, h->cfg.research, h->dOut);
+        ++h->launches;
+        check(cudaGetLastError(), "k_pack_records");
+        check(cudaMemcpyAsync(h->hOut, h->dOut, need, cudaMemcpyDeviceToHost, h->stream), "record download");
+        int cnt[4];
+        check(cudaMemcpyAsync(cnt, h->dCounters, sizeof(cnt), cudaMemcpyDeviceToHost, h->stream), "counters");
+        check(cudaStreamSynchronize(h->stream), "stage0 filter");
+        if (cnt[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
+        std::memcpy(out, h->hOut, need);
+        return BSF_OK;
+    });
+}
+
+int bsf_p20_filter(void* hv, const int64_t* seeds, uint32_t count, uint8_t* out, size_t outLen) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (!seeds || !out || count == 0 || count > static_cast<uint32_t>(h->capacity) || outLen < count)
+            throw std::invalid_argument("bsf_p20_filter: bad seeds/out/count");
+        const int n = static_cast<int>(count);
+        stage_seeds(h, seeds, n, true);
+        // The P20 count of centre 0 comes out of the fused Stage0 kernel; the
+        // stream protocol reports it for the world's first region only.
+        check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
+        launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, nullptr, h->dCounters, 0, h->stream);
+        k_pack_p20<<<(n + 255) / 256, 256, 0, h->stream>>>(h->dRegions, n, h->centers, h->dOut);
+        h->launches += 2;
+        check(cudaGetLastError(), "k_pack_p20");
+        check(cudaMemcpyAsync(h->hOut, h->dOut, count, cudaMemcpyDeviceToHost, h->stream), "download");
+        check(cudaStreamSynchronize(h->stream), "p20 filter");
+        std::memcpy(out, h->hOut, count);
+        return BSF_OK;
+    });
+}
+
+int bsf_chunk_bitmaps(void* hv, const int64_t* seeds, uint32_t count, int32_t chunkX, int32_t chunkZ,
+                      uint8_t* bitmaps, uint64_t* hashes) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (!seeds || !bitmaps || count == 0 || count > static_cast<uint32_t>(h->capacity))
+            throw std::invalid_argument("bsf_chunk_bitmaps: bad seeds/bitmaps/count");
+        if (chunkX < -(1 << 20) || chunkX > (1 << 20) || chunkZ < -(1 << 20) || chunkZ > (1 << 20))
+            throw std::invalid_argument("bsf_chunk_bitmaps: chunk coordinate out of range");
+        const int n = static_cast<int>(count);
+        stage_seeds(h, seeds, n, true);
+        launch_chunk_bitmaps(h->cache, n, chunkX, chunkZ, h->dOut, h->dHashes, h->stream);
+        ++h->launches;
+        check(cudaMemcpyAsync(h->hOut, h->dOut, static_cast<std::size_t>(n) * 4096, cudaMemcpyDeviceToHost, h->stream),
+              "bitmap download");
+        check(cudaStreamSynchronize(h->stream), "chunk bitmaps");
+        std::memcpy(bitmaps, h->hOut, static_cast<std::size_t>(n) * 4096);
+        if (hashes) check(cudaMemcpy(hashes, h->dHashes, static_cast<std::size_t>(n) * 8, cudaMemcpyDeviceToHost), "hashes");
+        return BSF_OK;
+    });
+}
+
+static int single_world(BsfHandle* h, int64_t seed) {
+    stage_seeds(h, &seed, 1, true);
+    return 0;
+}
+
+int bsf_exact_scan(void* hv, int64_t seed, int32_t ccx, int32_t ccz, int32_t radius, const bsf_match_settings* s,
+                   bsf_island* out) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (!out || radius < 0) throw std::invalid_argument("bsf_exact_scan: bad out/radius");
+        const int w = single_world(h, seed);
+        to_island(exact_once(h, w, ccx, ccz, radius, to_ms(s), false), out);
+        return BSF_OK;
+    });
+}
+
+int bsf_resolve_region(void* hv, int64_t seed, int32_t ccx, int32_t ccz, int32_t radius, int32_t coarse,
+                       const bsf_match_settings* s, bsf_island* out) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (!out || radius < 0) throw std::invalid_argument("bsf_resolve_region: bad out/radius");
+        if (h->exact.maxRadius < 24) throw std::length_error("bsf_resolve_region needs max_exact_radius 24");
+        const int w = single_world(h, seed);
+        to_island(resolve(h, w, ccx, ccz, radius, coarse, to_ms(s)), out);
+        return BSF_OK;
+    });
+}
+
+int bsf_preview(void* hv, int64_t seed, int32_t ccx, int32_t ccz, int32_t radius, const bsf_match_settings* s,
+                bsf_island* out, int32_t* minY, int32_t* maxY, uint32_t capacity) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (!out || !minY || !maxY || radius < 0) throw std::invalid_argument("bsf_preview: bad arguments");
+        const int w = single_world(h, seed);
+        const Island isl = exact_once(h, w, ccx, ccz, radius, to_ms(s), true);
+        to_island(isl, out);
+        if (!isl.found) return BSF_OK;
+        const std::size_t cells = static_cast<std::size_t>(isl.maxX - isl.minX + 1) * (isl.maxZ - isl.minZ + 1);
+        if (cells > capacity) throw std::length_error("bsf_preview: capacity smaller than the island footprint");
+        check(cudaMemcpy(minY, h->dPrevMin, cells * 4, cudaMemcpyDeviceToHost), "preview");
+        check(cudaMemcpy(maxY, h->dPrevMax, cells * 4, cudaMemcpyDeviceToHost), "preview");
+        return BSF_OK;
+    });
+}
+
+int bsf_mega_search(void* hv, const int64_t* seeds, uint32_t count, int32_t radius, const bsf_match_settings* s,
+                    bsf_mega_record* records, uint32_t recordsCap, uint32_t* recordsCount, bsf_stage_counts* counts) {
+    return guarded(hv, [&](BsfHandle* h) {
+        return mega_batch(h, seeds, true, nullptr, count, radius, s, records, recordsCap, recordsCount, counts);
+    });
+}
+
+int bsf_mega_search_device(void* hv, const int64_t* dSeeds, uint32_t count, int32_t radius,
+                           const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
+                           uint32_t* recordsCount, bsf_stage_counts* counts, void* stream) {
+    return guarded(hv, [&](BsfHandle* h) {
+        return mega_batch(h, dSeeds, false, static_cast<cudaStream_t>(stream), count, radius, s, records, recordsCap,
+                          recordsCount, counts);
+    });
+}
+
+uint64_t bsf_kernel_launches(const void* hv) {
+    const BsfHandle* h = static_cast<const BsfHandle*>(hv);
+    return h ? h->launches : 0;
+}
+
+}  // extern "C"

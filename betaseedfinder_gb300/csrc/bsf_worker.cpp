@@ -1,0 +1,261 @@
+// bsf_worker: drop-in for the reference worker executable's streaming modes.
+//
+//   bsf_worker stage0stream [capacity=32768] [general|mega|record60|record80] [research|lean] [centers=1|8]
+//   bsf_worker stream [capacity=32768]
+//   bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]
+//
+// stage0stream / stream keep the reference protocol byte for byte
+// (gpu_p20_benchmark.cpp:7310-7685; Java side src/GpuStage0Scout.java:143-335,
+// src/GpuP20Scout.java:45-93): an 8-byte magic on stdout at start, then per
+// request a LE u32 world count (0 or EOF ends the stream) and count LE i64 seeds
+// on stdin, answered by a LE u32 count and the records. Errors print
+// "ERROR: <message>" on stderr and exit 1; a closed stdout ends cleanly.
+// megastream is the new MEGA mode: same request framing, response = LE u32
+// record count followed by fixed 96-byte island records (see write_mega_record).
+#include "../../include/bsf.h"
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+bool read_exact(void* dst, std::size_t n) {
+    return std::fread(dst, 1, n, stdin) == n;
+}
+
+bool read_le32(std::uint32_t& v, bool& eof) {
+    unsigned char b[4];
+    const std::size_t got = std::fread(b, 1, 4, stdin);
+    if (got == 0 && std::feof(stdin)) {
+        eof = true;
+        return false;
+    }
+    if (got != 4) throw std::runtime_error("truncated stream request header");
+    v = static_cast<std::uint32_t>(b[0]) | (static_cast<std::uint32_t>(b[1]) << 8) |
+        (static_cast<std::uint32_t>(b[2]) << 16) | (static_cast<std::uint32_t>(b[3]) << 24);
+    return true;
+}
+
+void put_le32(std::vector<unsigned char>& o, std::uint32_t v) {
+    for (int k = 0; k < 4; ++k) o.push_back(static_cast<unsigned char>(v >> (8 * k)));
+}
+
+void put_le64(std::vector<unsigned char>& o, std::uint64_t v) {
+    for (int k = 0; k < 8; ++k) o.push_back(static_cast<unsigned char>(v >> (8 * k)));
+}
+
+bool write_all(const void* p, std::size_t n) {
+    if (std::fwrite(p, 1, n, stdout) != n) return false;
+    return std::fflush(stdout) == 0;
+}
+
+int parse_profile(const std::string& v) {
+    if (v == "general") return BSF_PROFILE_GENERAL;
+    if (v == "mega") return BSF_PROFILE_MEGA;
+    if (v == "record60") return BSF_PROFILE_RECORD60;
+    if (v == "record80") return BSF_PROFILE_RECORD80;
+    throw std::runtime_error("hunt profile must be general, mega, record60, or record80");
+}
+
+const char* profile_name(int p) {
+    static const char* names[] = {"GENERAL", "MEGA 30k+", "RECORD 60k+ (empirical)", "WORLD RECORD COARSE 700"};
+    return names[p];
+}
+
+struct Handle {
+    void* h = nullptr;
+    explicit Handle(const bsf_config& c) {
+        h = bsf_open(&c);
+        if (!h) throw std::runtime_error("out of memory opening the GPU worker");
+        if (bsf_last_error(h)[0] != '\0') throw std::runtime_error(bsf_last_error(h));
+    }
+    ~Handle() { bsf_close(h); }
+};
+
+std::vector<std::int64_t> read_seeds(std::uint32_t count) {
+    std::vector<std::int64_t> seeds(count);
+    std::vector<unsigned char> raw(static_cast<std::size_t>(count) * 8);
+    if (!read_exact(raw.data(), raw.size())) throw std::runtime_error("truncated stream seed batch");
+    for (std::uint32_t i = 0; i < count; ++i) {
+        std::uint64_t v = 0;
+        for (int k = 0; k < 8; ++k) v |= static_cast<std::uint64_t>(raw[i * 8 + k]) << (8 * k);
+        seeds[i] = static_cast<std::int64_t>(v);
+    }
+    return seeds;
+}
+
+int stage0stream(std::uint32_t capacity, int profile, bool research, int centers) {
+    if (capacity < 1) throw std::runtime_error("Stage0 stream capacity must be >= 1");
+    if (centers != 1 && centers != 8) throw std::runtime_error("Stage0 stream center count must be 1 or 8");
+    bsf_config cfg;
+    bsf_default_config(&cfg);
+    cfg.capacity = capacity;
+    cfg.profile = profile;
+    cfg.research = research ? 1 : 0;
+    cfg.centers = centers;
+    cfg.max_exact_radius = 1;
+    Handle h(cfg);
+    std::fprintf(stderr, "Stage0+P19+coarse stream capacity: %u worlds / %llu regions\n", capacity,
+                 static_cast<unsigned long long>(capacity) * centers);
+    std::fprintf(stderr, "GB300 worker profile: %s | fused P20/Upper/Lower/P19 kernel, device-queued coarse\n",
+                 profile_name(profile));
+    std::fprintf(stderr, "Response telemetry: %s\n",
+                 research ? "RESEARCH 34 bytes/region" : "LEAN 16 bytes/region + exact P19 double");
+    const std::size_t rec = research ? 34 : 16;
+    const char magic[8] = {'S', 'T', '0', 'R', '3', '8', '1', '6'};
+    if (!write_all(magic, 8)) return 0;
+    std::vector<unsigned char> out;
+    unsigned long long worlds = 0;
+    for (;;) {
+        std::uint32_t count = 0;
+        bool eof = false;
+        if (!read_le32(count, eof) || count == 0) break;
+        if (count > capacity) throw std::runtime_error("Stage0 stream batch exceeds configured world capacity");
+        const std::vector<std::int64_t> seeds = read_seeds(count);
+        out.assign(4 + static_cast<std::size_t>(count) * centers * rec, 0);
+        out[0] = static_cast<unsigned char>(count);
+        out[1] = static_cast<unsigned char>(count >> 8);
+        out[2] = static_cast<unsigned char>(count >> 16);
+        out[3] = static_cast<unsigned char>(count >> 24);
+        const int st = bsf_stage0_filter(h.h, seeds.data(), count, out.data() + 4, out.size() - 4);
+        if (st != BSF_OK) throw std::runtime_error(bsf_last_error(h.h));
+        if (!write_all(out.data(), out.size())) {
+            std::fprintf(stderr, "Stage0+P19+coarse stream parent closed response pipe; exiting cleanly\n");
+            break;
+        }
+        worlds += count;
+    }
+    std::fprintf(stderr, "Stage0+P19+coarse stream closed | worlds=%llu | regions=%llu\n", worlds,
+                 worlds * static_cast<unsigned long long>(centers));
+    return 0;
+}
+
+int p20stream(std::uint32_t capacity) {
+    if (capacity < 1) throw std::runtime_error("stream capacity must be >= 1");
+    bsf_config cfg;
+    bsf_default_config(&cfg);
+    cfg.capacity = capacity;
+    cfg.centers = 1;
+    cfg.profile = BSF_PROFILE_GENERAL;
+    cfg.max_exact_radius = 1;
+    Handle h(cfg);
+    std::fprintf(stderr, "P20 stream capacity: %u seeds\n", capacity);
+    const char magic[8] = {'P', '2', '0', 'S', 'T', 'R', '0', '1'};
+    if (!write_all(magic, 8)) return 0;
+    std::vector<unsigned char> out;
+    unsigned long long seedsTotal = 0, passed = 0;
+    for (;;) {
+        std::uint32_t count = 0;
+        bool eof = false;
+        if (!read_le32(count, eof) || count == 0) break;
+        if (count > capacity) throw std::runtime_error("stream batch exceeds configured capacity");
+        const std::vector<std::int64_t> seeds = read_seeds(count);
+        out.assign(4 + count, 0);
+        for (int k = 0; k < 4; ++k) out[k] = static_cast<unsigned char>(count >> (8 * k));
+        if (bsf_p20_filter(h.h, seeds.data(), count, out.data() + 4, count) != BSF_OK)
+            throw std::runtime_error(bsf_last_error(h.h));
+        for (std::uint32_t i = 0; i < count; ++i) passed += out[4 + i] > 0;
+        if (!write_all(out.data(), out.size())) throw std::runtime_error("failed writing stream response");
+        seedsTotal += count;
+    }
+    std::fprintf(stderr, "P20 stream closed | seeds=%llu | passed=%llu\n", seedsTotal, passed);
+    return 0;
+}
+
+// 96-byte MEGA record: seed i64, world u32, centre u32, centre chunk x/z i32,
+// p20/upper/high/coarse i32, P19 score f64 bits, island found/blocks/columns,
+// minX/maxX/minZ/maxZ/minY/maxY, centerX/centerZ, touchesSide, radiusUsed i32.
+void write_mega_record(std::vector<unsigned char>& o, const bsf_mega_record& r) {
+    put_le64(o, static_cast<std::uint64_t>(r.seed));
+    put_le32(o, static_cast<std::uint32_t>(r.world_index));
+    put_le32(o, static_cast<std::uint32_t>(r.center_index));
+    put_le32(o, static_cast<std::uint32_t>(r.center_chunk_x));
+    put_le32(o, static_cast<std::uint32_t>(r.center_chunk_z));
+    put_le32(o, static_cast<std::uint32_t>(r.p20));
+    put_le32(o, static_cast<std::uint32_t>(r.upper));
+    put_le32(o, static_cast<std::uint32_t>(r.high));
+    put_le32(o, static_cast<std::uint32_t>(r.coarse));
+    std::uint64_t bits;
+    std::memcpy(&bits, &r.p19_score, 8);
+    put_le64(o, bits);
+    const bsf_island& i = r.island;
+    const std::int32_t f[14] = {i.found, i.blocks, i.columns, i.min_x, i.max_x, i.min_z, i.max_z,
+                                i.min_y, i.max_y, i.center_x, i.center_z, i.touches_side, i.radius_used, 0};
+    for (std::int32_t v : f) put_le32(o, static_cast<std::uint32_t>(v));
+}
+
+int megastream(std::uint32_t capacity, int profile, int radius) {
+    bsf_config cfg;
+    bsf_default_config(&cfg);
+    cfg.capacity = capacity;
+    cfg.profile = profile;
+    cfg.centers = 8;
+    Handle h(cfg);
+    std::fprintf(stderr, "MEGA stream capacity: %u worlds | profile %s | exact radius %d\n", capacity,
+                 profile_name(profile), radius);
+    const char magic[8] = {'M', 'E', 'G', 'A', 'S', 'T', '0', '1'};
+    if (!write_all(magic, 8)) return 0;
+    std::vector<bsf_mega_record> recs(65536);
+    for (;;) {
+        std::uint32_t count = 0;
+        bool eof = false;
+        if (!read_le32(count, eof) || count == 0) break;
+        if (count > capacity) throw std::runtime_error("MEGA stream batch exceeds configured world capacity");
+        const std::vector<std::int64_t> seeds = read_seeds(count);
+        std::uint32_t n = 0;
+        bsf_stage_counts counts;
+        if (bsf_mega_search(h.h, seeds.data(), count, radius, nullptr, recs.data(),
+                            static_cast<std::uint32_t>(recs.size()), &n, &counts) != BSF_OK)
+            throw std::runtime_error(bsf_last_error(h.h));
+        std::vector<unsigned char> out;
+        put_le32(out, n);
+        for (std::uint32_t k = 0; k < n; ++k) write_mega_record(out, recs[k]);
+        if (!write_all(out.data(), out.size())) break;
+    }
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    try {
+        if (argc < 2) {
+            std::fprintf(stderr,
+                         "Usage:\n"
+                         "  bsf_worker stage0stream [capacity=32768] [general|mega|record60|record80] [research|lean] "
+                         "[centers=1|8]\n"
+                         "  bsf_worker stream [capacity=32768]\n"
+                         "  bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]\n");
+            return 1;
+        }
+        const std::string mode = argv[1];
+        const std::uint32_t cap = argc > 2 ? static_cast<std::uint32_t>(std::strtoul(argv[2], nullptr, 10)) : 32768u;
+        if (mode == "stream") return p20stream(cap);
+        if (mode == "stage0stream") {
+            const int profile = argc > 3 ? parse_profile(argv[3]) : BSF_PROFILE_GENERAL;
+            bool research = true;
+            if (argc > 4) {
+                const std::string t = argv[4];
+                if (t == "research") research = true;
+                else if (t == "lean") research = false;
+                else throw std::runtime_error("stage0stream telemetry must be research or lean");
+            }
+            const int centers = argc > 5 ? std::atoi(argv[5]) : 1;
+            return stage0stream(cap, profile, research, centers);
+        }
+        if (mode == "megastream") {
+            const int profile = argc > 3 ? parse_profile(argv[3]) : BSF_PROFILE_MEGA;
+            const int radius = argc > 4 ? std::atoi(argv[4]) : 7;
+            return megastream(cap, profile, radius);
+        }
+        throw std::runtime_error("unknown mode: " + mode);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "ERROR: %s\n", e.what());
+        return 1;
+    }
+}

@@ -1,0 +1,147 @@
+/*
+ * libbsf: GB300 (sm_103a) Beta 1.7.3 floating-island seed-finder worker, C ABI.
+ *
+ * Plain C types only; all buffers are caller-owned host memory unless the
+ * name ends in _device (device pointers + a cudaStream_t passed as void*).
+ * Every function returns BSF_OK (0) or a negative BSF_E_* status; the message
+ * of the last failure on a handle is available from bsf_last_error(). No C++
+ * exception crosses this boundary. A handle serves one request at a time
+ * (the reference worker is single-request too: GpuStage0Scout.filter is
+ * synchronized, src/GpuStage0Scout.java:249); use one handle per thread.
+ */
+#ifndef BSF_H
+#define BSF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BSF_OK 0
+#define BSF_E_ARG (-1)     /* invalid argument (null pointer, bad size, count > capacity) */
+#define BSF_E_CUDA (-2)    /* CUDA runtime failure */
+#define BSF_E_STATE (-3)   /* handle unusable (open failed or a device fault occurred) */
+#define BSF_E_LIMIT (-4)   /* request exceeds a provisioned limit (radius, preview size) */
+
+/* Hunt profiles: gpu_p20_benchmark.cpp:7251-7298 (HuntProfileConfig). */
+#define BSF_PROFILE_GENERAL 0
+#define BSF_PROFILE_MEGA 1
+#define BSF_PROFILE_RECORD60 2
+#define BSF_PROFILE_RECORD80 3
+
+/* Pipeline forms for the batch entry points. */
+#define BSF_MODE_QUEUED 0 /* fused Stage0 kernel, device-side queues, one host sync per batch */
+#define BSF_MODE_PLAIN 1  /* one launch per stage, host round trip after every stage */
+
+typedef struct bsf_config {
+    int32_t device;           /* CUDA device ordinal */
+    uint32_t capacity;        /* max worlds per request; worker argv "capacity" (default 32768) */
+    int32_t profile;          /* BSF_PROFILE_* (worker argv profile) */
+    int32_t research;         /* 1: 34-byte research records, 0: 16-byte lean records */
+    int32_t centers;          /* regions per world: 1 or 8 (worker argv "centers") */
+    int32_t max_exact_radius; /* largest exact-scan radius to provision (24 covers border verify) */
+} bsf_config;
+
+/* SearchSettings match thresholds (src/SearchSettings.java:39-45). */
+typedef struct bsf_match_settings {
+    int32_t min_blocks, min_columns, min_y_for_match, min_width, min_depth;
+    double min_avg_thickness;
+} bsf_match_settings;
+
+/* IslandSearchEngine.Component (src/IslandSearchEngine.java:6516-6536) of the chosen island. */
+typedef struct bsf_island {
+    int32_t found;
+    int32_t blocks, columns;
+    int32_t min_x, max_x, min_z, max_z, min_y, max_y;
+    int32_t center_x, center_z;
+    int32_t touches_side, touches_bottom;
+    int32_t radius_used;
+    int64_t sum_x, sum_z;
+} bsf_island;
+
+/* One region that reached the exact stage in bsf_mega_search. */
+typedef struct bsf_mega_record {
+    int64_t seed;
+    int32_t world_index;    /* index into the request's seed array */
+    int32_t center_index;   /* 0..7 (GpuStage0Scout centres) */
+    int32_t center_chunk_x, center_chunk_z;
+    int32_t p20, upper, high, coarse;
+    double p19_score;
+    bsf_island island;      /* found == 0 when no island matched */
+} bsf_mega_record;
+
+typedef struct bsf_stage_counts {
+    uint64_t worlds, regions, p20_passed, upper_passed, high_passed, p19_passed,
+             mega_rejected, coarse_evaluated, coarse_passed, islands, rng_fallbacks;
+} bsf_stage_counts;
+
+/* Lifecycle. bsf_open returns NULL only when allocation of the handle itself fails;
+ * check bsf_last_error(h) for an open failure (then every call returns BSF_E_STATE). */
+void bsf_default_config(bsf_config* cfg);
+void bsf_default_match_settings(bsf_match_settings* s);
+void* bsf_open(const bsf_config* cfg);
+void bsf_close(void* h);
+const char* bsf_last_error(const void* h);
+int bsf_set_mode(void* h, int32_t mode);
+
+/* Stage0 scout batch: the worker's `stage0stream` response body for `count`
+ * worlds (gpu_p20_benchmark.cpp:7310-7613 streamStage0Filter; Java caller
+ * GpuStage0Scout.filter, src/GpuStage0Scout.java:249-335). Writes
+ * count * centers records of 16 (lean) or 34 (research) bytes, world-major,
+ * centre-minor, into out (out_len must hold them). */
+int bsf_stage0_filter(void* h, const int64_t* seeds, uint32_t count, uint8_t* out, size_t out_len);
+
+/* P20-only batch: the worker's `stream` response body, one clamped P20 count
+ * byte per seed (gpu_p20_benchmark.cpp:7614-7685 streamFilter; Java caller
+ * GpuP20Scout, src/GpuP20Scout.java:45-93). */
+int bsf_p20_filter(void* h, const int64_t* seeds, uint32_t count, uint8_t* out, size_t out_len);
+
+/* BetaTerrain173.generateChunkBaseTerrain (src/beta173/BetaTerrain173.java:120-138)
+ * reduced to a stone bitmap: bit (x*16+z)*128+y of 4096 bytes per seed, LSB
+ * first, plus a 64-bit hash per bitmap (sum over the 512 little-endian words w_i
+ * of splitmix64-finalizer(w_i + (i+1) * 0x9E3779B97F4A7C15)). */
+int bsf_chunk_bitmaps(void* h, const int64_t* seeds, uint32_t count, int32_t chunk_x, int32_t chunk_z,
+                      uint8_t* bitmaps, uint64_t* hashes);
+
+/* Exact-only findFloatingIslandInSeed at one radius around a centre chunk
+ * (src/IslandSearchEngine.java:2861-2977), no border verify or hot scan. */
+int bsf_exact_scan(void* h, int64_t seed, int32_t center_chunk_x, int32_t center_chunk_z, int32_t radius,
+                   const bsf_match_settings* s, bsf_island* out);
+
+/* processGpuRegionAttempt (src/IslandSearchEngine.java:1878-1971): exact scan at
+ * `radius` with side-border verification (radii 10,13,16,20,24) and the
+ * radius-16 hot scan when coarse >= 120; returns the reference's chosen island. */
+int bsf_resolve_region(void* h, int64_t seed, int32_t center_chunk_x, int32_t center_chunk_z, int32_t radius,
+                       int32_t coarse, const bsf_match_settings* s, bsf_island* out);
+
+/* buildIsland3DData (src/IslandSearchEngine.java:389-436; src/Island3DData.java):
+ * the best island of an exact scan and its per-column lowest/highest stone Y over
+ * its bounding box (index x*depth+z; INT32_MAX / INT32_MIN for empty columns).
+ * capacity = entries available in min_y / max_y. */
+int bsf_preview(void* h, int64_t seed, int32_t center_chunk_x, int32_t center_chunk_z, int32_t radius,
+                const bsf_match_settings* s, bsf_island* out, int32_t* min_y, int32_t* max_y, uint32_t capacity);
+
+/* Whole MEGA pipeline for a batch of worlds: Stage0 (P20 -> Upper -> Lower) ->
+ * P19 + Mega topology -> coarse -> exact scan (+ border verify + hot scan) for
+ * regions whose coarse score reaches the profile threshold. Writes one record
+ * per exact-stage region (in world, centre order) up to records_cap. */
+int bsf_mega_search(void* h, const int64_t* seeds, uint32_t count, int32_t radius, const bsf_match_settings* s,
+                    bsf_mega_record* records, uint32_t records_cap, uint32_t* records_count,
+                    bsf_stage_counts* counts);
+
+/* Device-resident variant of bsf_mega_search's GPU stages for callers that keep
+ * seeds in HBM: d_seeds is a device pointer, stream a cudaStream_t (NULL =
+ * the handle's stream). Exact-stage regions are returned like bsf_mega_search. */
+int bsf_mega_search_device(void* h, const int64_t* d_seeds, uint32_t count, int32_t radius,
+                           const bsf_match_settings* s, bsf_mega_record* records, uint32_t records_cap,
+                           uint32_t* records_count, bsf_stage_counts* counts, void* stream);
+
+/* Number of GPU kernel launches issued by the handle so far (instrumentation). */
+uint64_t bsf_kernel_launches(const void* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
