@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Benchmark: worlds (seeds) per second through every MEGA-profile stage on GB300.
+
+One step = one batch of consecutive world seeds (default 32768 worlds = 262,144
+regions at 8 centres) through generator setup -> Stage0 (P20 -> Upper ->
+Lower) -> P19 + Mega topology -> coarse 61x61x17 score -> exact 16x128x16
+terrain scan (+ border verify + hot scan) for coarse survivors. Seeds are
+seeded synthetic consecutive 48-bit values (the full-pipeline workload over
+2^36 consecutive seeds, sampled one batch per step).
+
+  value  : worlds/s with seeds already resident in HBM (bsf_mega_search_device),
+           CUDA events on the stream the kernels run on.
+  e2e    : worlds/s through bsf_mega_search with host seeds (H2D + D2H inside).
+  --impl reference : the CPU restatement of the reference pipeline (oracle) on
+           all host cores, one bounded sample per step.
+Under torchrun each rank takes its own seed range (weak scaling, no collective
+on the data path; a barrier and a max-reduce of the timings only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GOLDEN = 0x9E3779B97F4A7C15
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="bsf", choices=["bsf", "reference"])
+    p.add_argument("--batch", type=int, default=32768)
+    p.add_argument("--profile", default="mega")
+    p.add_argument("--radius", type=int, default=7)
+    p.add_argument("--seed", type=int, default=20261203)
+    p.add_argument("--plain-steps", type=int, default=2)
+    p.add_argument("--cpu-sample", type=int, default=1024, help="worlds for the CPU baseline sample")
+    p.add_argument("--ref-sample", type=int, default=256, help="worlds per reference-arm step")
+    p.add_argument("--previews", type=int, default=30)
+    p.add_argument("--skip-extras", action="store_true")
+    return p.parse_args()
+
+
+def splitmix(seq, attempt):
+    m = (1 << 64) - 1
+    z = (seq + attempt * GOLDEN) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return z ^ (z >> 31)
+
+
+def seed_start(seed, rank, stream_id):
+    """A seeded random 48-bit start for a rank's consecutive seed range."""
+    return splitmix(seed, rank * 16 + stream_id) & ((1 << 47) - 1)
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_ops(device):
+    """Measured FP64 issue rate of this GPU: cuBLAS DGEMM (torch) FLOP/s / 2, i.e.
+    one DADD/DMUL/DFMA per FP64 lane per cycle (the kernels issue no FMAs)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) / 1e3))
+    return best / 2.0, best
+
+
+# Algorithmic FP64 operations (IEEE add/sub/mul/div, each 1) of one lattice
+# column, following the reference formulas: per 3D octave 2 coordinate axes
+# (scale, offset, fraction, minus-one, fade = 11 each), 21 per Y cell
+# (8 gradient adds, y-1, 4 lerps of 3), 11 per Y sample (3 lerps, weight,
+# accumulate); per 2D octave 37; per simplex octave 60 and 20 for the climate
+# formula; 25 for the column shape; 12 per density level.
+def _cells(n_levels, sy):
+    return n_levels if sy >= 1.0 else min(n_levels, 1.0 + (n_levels - 1) * sy)
+
+
+def column_fp64_ops(n_levels):
+    ops = 0.0
+    for k in range(16):
+        sy = 684.412 / 2 ** k
+        ops += 2 * (22 + 21 * _cells(n_levels, sy) + 11 * n_levels)
+    for k in range(8):
+        sy = 684.412 / 160.0 / 2 ** k
+        ops += 22 + 21 * _cells(n_levels, sy) + 11 * n_levels
+    return ops + 12 * n_levels
+
+
+SHAPE_OPS = 26 * 37 + 10 * 60 + 20 + 25
+
+
+def stage0_fp64_ops(c):
+    """Stage0+P19 kernel FP64 ops of a batch from its stage counts."""
+    regions = c["regions"]
+    up_cols = regions * 64 + c["p20_passed"] * 192
+    return up_cols * (column_fp64_ops(6) + SHAPE_OPS) + c["lower_columns"] * (
+        0.5 * column_fp64_ops(6) + 0.5 * column_fp64_ops(5))
+
+
+def cpu_baseline(args, seeds_start, n_worlds):
+    from oracle import pyoracle as po
+    import numpy as np
+    po.build()
+    threads = os.cpu_count() or 1
+    seeds = np.arange(seeds_start, seeds_start + n_worlds, dtype=np.int64)
+    t0 = time.perf_counter()
+    counts, islands, _ = po.mega_pipeline(seeds, profile=1, radius=args.radius, threads=threads)
+    dt = time.perf_counter() - t0
+    return n_worlds / dt, threads, dt, counts
+
+
+def run_reference(args, dist):
+    """CPU reference arm: the oracle restatement of the reference pipeline on all host cores."""
+    if dist.rank != 0:
+        return
+    import numpy as np
+    from oracle import pyoracle as po
+    po.build()
+    threads = os.cpu_count() or 1
+    start = seed_start(args.seed, 0, 1)
+    for w in range(args.warmup):
+        s = np.arange(start + w * args.ref_sample, start + (w + 1) * args.ref_sample, dtype=np.int64)
+        po.mega_pipeline(s, profile=1, radius=args.radius, threads=threads)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        base = start + (args.warmup + k) * args.ref_sample
+        s = np.arange(base, base + args.ref_sample, dtype=np.int64)
+        po.mega_pipeline(s, profile=1, radius=args.radius, threads=threads)
+    dt = time.perf_counter() - t0
+    v = args.ref_sample * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "seeds_per_s_mega_pipeline", "value": v, "unit": "worlds/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "mega_pipeline_consecutive_48bit_seeds", "profile": args.profile,
+                   "centers": 8, "exact_radius": args.radius, "worlds_per_step": args.ref_sample},
+        "cpu_baseline": {"value": v, "unit": "worlds/s", "cores": threads, "kind": "port",
+                         "sample": "%d consecutive worlds x 8 centres per step" % args.ref_sample},
+        "e2e": {"value": v, "unit": "worlds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        dist.close()
+        return
+    import numpy as np
+    import torch
+    import betaseedfinder_gb300 as bsf
+    from betaseedfinder_gb300 import build as bsf_build
+    if dist.rank == 0:
+        bsf_build.build()
+    dist.barrier()
+    device = torch.device("cuda", dist.local)
+    torch.cuda.set_device(device)
+    B, K, W = args.batch, args.steps, args.warmup
+    worker = bsf.Worker(capacity=B, profile=args.profile, centers=8, max_exact_radius=24, device=dist.local)
+    start = seed_start(args.seed, dist.rank, 0)
+    steps_total = W + K
+    d_seeds = (torch.arange(steps_total * B, dtype=torch.int64, device=device) + start).view(steps_total, B)
+    stream = torch.cuda.current_stream(device)
+    sptr = stream.cuda_stream
+
+    for s in range(W):
+        worker.mega_search_device(d_seeds[s].data_ptr(), B, radius=args.radius, stream=sptr)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    time.sleep(0.4)
+    dist.barrier()
+    torch.cuda.synchronize()
+    l0 = worker.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    totals = None
+    stage = [0.0, 0.0, 0.0, 0.0]
+    records = 0
+    for s in range(K):
+        counts, recs = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+        d = counts.as_dict()
+        totals = d if totals is None else {k: totals[k] + d[k] for k in d}
+        st = worker.last_stage_ms()
+        stage = [a + b for a, b in zip(stage, st)]
+        records += len(recs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = worker.kernel_launches - l0
+    clk = clocks.stop()
+    ms_max = dist.max(ms)
+    value = B * K * dist.world / (ms_max / 1e3)
+
+    # e2e: host seeds through the public API (H2D seeds, D2H counts + records inside).
+    host_start = seed_start(args.seed, dist.rank, 2)
+    host_blocks = [np.arange(host_start + s * B, host_start + (s + 1) * B, dtype=np.int64) for s in range(K + 1)]
+    worker.mega_search(host_blocks[K], radius=args.radius)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_records = 0
+    for s in range(K):
+        _, recs = worker.mega_search(host_blocks[s], radius=args.radius)
+        e2e_records += len(recs)
+    torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = B * K * dist.world / e2e_s
+    rec_bytes = __import__("ctypes").sizeof(bsf.MegaRecord)
+    d2h = 8 * 8 + 4 * 4 + (e2e_records / max(1, K)) * (rec_bytes + 48)
+
+    extras = {}
+    if dist.rank == 0 and not args.skip_extras:
+        # plain stage-by-stage form on the same workload (spec comparison)
+        worker.set_mode(bsf.MODE_PLAIN)
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        for s in range(args.plain_steps):
+            worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+        torch.cuda.synchronize()
+        plain = B * args.plain_steps / (time.perf_counter() - p0)
+        worker.set_mode(bsf.MODE_QUEUED)
+        extras["forms"] = {"queued_worlds_per_s": value / dist.world, "plain_worlds_per_s": plain,
+                           "queued_over_plain": (value / dist.world) / plain}
+        # single-seed island previews (served request class): latency per preview
+        lat = []
+        for i in range(args.previews):
+            t = time.perf_counter()
+            worker.preview(int(splitmix(args.seed, 1000 + i) & ((1 << 48) - 1)), 0, 0, args.radius)
+            lat.append((time.perf_counter() - t) * 1e3)
+        lat.sort()
+        extras["preview_ms"] = {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                                "n": len(lat), "radius": args.radius}
+
+    if dist.rank == 0:
+        stage0_ms = stage[1] / K
+        ops = stage0_fp64_ops(totals) / K
+        peak_ops, dgemm = fp64_peak_ops(device)
+        achieved = ops / (stage0_ms / 1e3)
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "stage0_traffic.json")
+        if os.path.exists(tpath):
+            try:
+                t = json.load(open(tpath))
+                traffic = t.get("bytes_per_world", 0) * B
+            except (ValueError, OSError):
+                traffic = None
+        cpu = None
+        if not args.skip_extras:
+            v, cores, dt, _ = cpu_baseline(args, seed_start(args.seed, 0, 3), args.cpu_sample)
+            cpu = {"value": v, "unit": "worlds/s", "cores": cores, "kind": "port",
+                   "sample": "%d consecutive worlds x 8 centres, full MEGA pipeline, %.1f s" % (args.cpu_sample, dt)}
+        line = {
+            "metric": "seeds_per_s_mega_pipeline", "value": value, "unit": "worlds/s", "n_gpus": dist.world,
+            "steps": K, "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mega_pipeline_consecutive_48bit_seeds", "profile": args.profile,
+                       "worlds_per_step": B, "regions_per_step": B * 8, "centers": 8, "exact_radius": args.radius,
+                       "l2": "per-step working set (generator cache %.0f MB) exceeds L2" % (B * 21888 / 1e6)},
+            "e2e": {"value": e2e_value, "unit": "worlds/s", "h2d_bytes_per_step": B * 8,
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "kernel": "k_stage0", "achieved": achieved / 1e12,
+                         "peak": peak_ops / 1e12, "unit": "TFLOP/s", "frac": achieved / peak_ops,
+                         "traffic": traffic, "peak_source": "measured live: cuBLAS DGEMM %.3f TFLOP/s / 2 "
+                                                            "(non-fused FP64 ops)" % (dgemm / 1e12)},
+            "stage_ms_per_step": {"setup": stage[0] / K, "stage0": stage0_ms, "coarse": stage[2] / K,
+                                  "exact_host": stage[3] / K},
+            "stage_counts": totals, "exact_records": records,
+            "clocks": clk,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        line.update(extras)
+        print(json.dumps(line))
+    worker.close()
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -62,7 +62,7 @@ class MegaRecord(ctypes.Structure):
 class StageCounts(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "worlds", "regions", "p20_passed", "upper_passed", "high_passed", "p19_passed",
-        "mega_rejected", "coarse_evaluated", "coarse_passed", "islands", "rng_fallbacks")]
+        "mega_rejected", "coarse_evaluated", "coarse_passed", "islands", "rng_fallbacks", "lower_columns")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -71,7 +71,7 @@ class StageCounts(ctypes.Structure):
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
-           "bsf_kernel_launches"]
+           "bsf_kernel_launches", "bsf_last_stage_ms"]
 
 _lib = None
 
@@ -110,6 +110,7 @@ def load(path=LIB_PATH):
                                          ctypes.c_void_p]
     L.bsf_kernel_launches.argtypes = [vp]
     L.bsf_kernel_launches.restype = ctypes.c_uint64
+    L.bsf_last_stage_ms.argtypes = [vp, P(ctypes.c_float)]
     _lib = L
     return L
 
@@ -176,6 +177,12 @@ class Worker:
     @property
     def kernel_launches(self):
         return int(load().bsf_kernel_launches(self._h))
+
+    def last_stage_ms(self):
+        """Per-stage device times of the last batch: setup, Stage0+P19, coarse, exact (ms)."""
+        ms = (ctypes.c_float * 4)()
+        self._check(load().bsf_last_stage_ms(self._h, ms))
+        return list(ms)
 
     def set_mode(self, mode):
         self._check(load().bsf_set_mode(self._h, mode))

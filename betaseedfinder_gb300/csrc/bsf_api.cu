@@ -5,6 +5,7 @@
 #include "bsf_internal.h"
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -77,7 +78,7 @@ __global__ void k_stage_counts(const RegionInfo* __restrict__ regions, int count
                                unsigned long long* counts, RegionRef* exactQueue, int* exactCount, int exactCap,
                                int centers) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
+    unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < count) {
         const RegionInfo r = regions[i];
         const bool p20 = r.p20 >= prof.p20MinCount;
@@ -90,13 +91,14 @@ __global__ void k_stage_counts(const RegionInfo* __restrict__ regions, int count
         c[4] = hi && r.p19Pass && r.megaReject;
         c[5] = r.coarseEvaluated;
         c[6] = r.coarseEvaluated && r.coarse >= prof.coarseMinCells;
+        c[7] = up ? static_cast<unsigned long long>(r.upper) : 0ULL;  // Lower-stage columns
         if (c[6]) {
             const int slot = atomicAdd(exactCount, 1);
             if (slot < exactCap) exactQueue[slot] = RegionRef{i / centers, i % centers};
         }
     }
 #pragma unroll
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 8; ++k) {
         unsigned long long v = c[k];
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd(&counts[k], v);
@@ -143,6 +145,8 @@ struct BsfHandle {
     std::uint8_t* hOut = nullptr;
     std::size_t outBytes = 0;
     std::vector<RegionInfo> hRegions;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    float stageMs[4] = {0, 0, 0, 0};
 
     void alloc(void** p, std::size_t bytes, const char* what) { check(cudaMalloc(p, bytes), what); }
 };
@@ -260,6 +264,32 @@ void run_gpu_stages(BsfHandle* h, int n) {
     else run_gpu_stages_queued(h, n);
 }
 
+void record(BsfHandle* h, int i) { check(cudaEventRecord(h->ev[i], h->stream), "event"); }
+
+// Stage0 and coarse bracketed by events (event 2 sits between them in the
+// queued form; in the plain form the host round trips fall inside stage 1/2).
+void run_gpu_stages_timed(BsfHandle* h, int n) {
+    if (h->mode == BSF_MODE_PLAIN) {
+        run_gpu_stages_plain(h, n);
+        record(h, 2);
+        record(h, 3);
+        return;
+    }
+    check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
+    launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, h->dCoarseQueue, h->dCounters,
+                  h->capacity * h->centers, h->stream);
+    record(h, 2);
+    launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, LatticeBuffers{}, h->dSigns,
+                        h->dLabels, h->dStats, h->dRegions, h->centers, h->stream);
+    record(h, 3);
+    h->launches += 3;
+}
+
+void read_stage_times(BsfHandle* h) {
+    for (int i = 0; i < 2; ++i) check(cudaEventElapsedTime(&h->stageMs[i], h->ev[i], h->ev[i + 1]), "event time");
+    check(cudaEventElapsedTime(&h->stageMs[2], h->ev[2], h->ev[3]), "event time");
+}
+
 Island exact_once(BsfHandle* h, int world, int ccx, int ccz, int radius, const MatchSettings& ms, bool preview) {
     if (radius > h->exact.maxRadius) throw std::length_error("exact radius exceeds the provisioned max_exact_radius");
     launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, h->exact, h->dIsland, preview ? h->dPrevMin : nullptr,
@@ -331,8 +361,10 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     const int n = static_cast<int>(count);
     check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
     check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
+    record(h, 0);
     stage_seeds(h, seeds, n, hostSeeds);
-    run_gpu_stages(h, n);
+    record(h, 1);
+    run_gpu_stages_timed(h, n);
     const int regions = n * h->centers;
     k_stage_counts<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, h->prof, h->dStageCounts,
                                                                 h->dExactQueue, h->dCounters + 2, h->exactCap,
@@ -345,6 +377,8 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     check(cudaMemcpyAsync(hcount, h->dCounters, sizeof(hcount), cudaMemcpyDeviceToHost, h->stream), "counts");
     check(cudaStreamSynchronize(h->stream), "mega batch");
     if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
+    read_stage_times(h);
+    const auto exactStart = std::chrono::steady_clock::now();
     const int exactN = std::min(hcount[2], h->exactCap);
     std::vector<RegionRef> ex(exactN);
     std::vector<RegionInfo> info(exactN);
@@ -382,6 +416,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
             to_island(isl, &r.island);
         }
     }
+    h->stageMs[3] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - exactStart).count();
     if (recordsCount) *recordsCount = written;
     if (counts) {
         counts->worlds = count;
@@ -395,6 +430,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
         counts->coarse_passed = hc[6];
         counts->islands = islands;
         counts->rng_fallbacks = static_cast<uint64_t>(hcount[1]);
+        counts->lower_columns = hc[7];
     }
     h->stream = saved;
     return BSF_OK;
@@ -472,6 +508,7 @@ void* bsf_open(const bsf_config* cfgIn) {
         h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
         h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
         h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+        for (auto& e : h->ev) check(cudaEventCreate(&e), "event");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hSeeds), n * 8), "pinned seeds");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
               "pinned output");
@@ -493,6 +530,8 @@ void bsf_close(void* hv) {
                    h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax};
     for (void* p : dev)
         if (p) cudaFree(p);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
     if (h->hSeeds) cudaFreeHost(h->hSeeds);
     if (h->hOut) cudaFreeHost(h->hOut);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -634,6 +673,13 @@ int bsf_mega_search_device(void* hv, const int64_t* dSeeds, uint32_t count, int3
         return mega_batch(h, dSeeds, false, static_cast<cudaStream_t>(stream), count, radius, s, records, recordsCap,
                           recordsCount, counts);
     });
+}
+
+int bsf_last_stage_ms(const void* hv, float* ms4) {
+    const BsfHandle* h = static_cast<const BsfHandle*>(hv);
+    if (!h || !ms4) return BSF_E_ARG;
+    for (int i = 0; i < 4; ++i) ms4[i] = h->stageMs[i];
+    return BSF_OK;
 }
 
 uint64_t bsf_kernel_launches(const void* hv) {

@@ -74,7 +74,8 @@ typedef struct bsf_mega_record {
 
 typedef struct bsf_stage_counts {
     uint64_t worlds, regions, p20_passed, upper_passed, high_passed, p19_passed,
-             mega_rejected, coarse_evaluated, coarse_passed, islands, rng_fallbacks;
+             mega_rejected, coarse_evaluated, coarse_passed, islands, rng_fallbacks,
+             lower_columns; /* lattice columns evaluated by the Lower stage */
 } bsf_stage_counts;
 
 /* Lifecycle. bsf_open returns NULL only when allocation of the handle itself fails;
@@ -140,6 +141,12 @@ int bsf_mega_search_device(void* h, const int64_t* d_seeds, uint32_t count, int3
 
 /* Number of GPU kernel launches issued by the handle so far (instrumentation). */
 uint64_t bsf_kernel_launches(const void* h);
+
+/* Device time of each stage of the last batch call, from CUDA events recorded
+ * on the stream the kernels ran on (instrumentation): ms[0] generator setup,
+ * ms[1] Stage0 + P19, ms[2] coarse, ms[3] exact stage (host wall time, it
+ * includes its round trips). */
+int bsf_last_stage_ms(const void* h, float* ms4);
 
 #ifdef __cplusplus
 }
