@@ -218,12 +218,21 @@ void stage_seeds(BsfHandle* h, const std::int64_t* seeds, int n, bool hostSeeds)
 
 // Queued form: fused Stage0 kernel appends P19 survivors to the device coarse
 // queue; the coarse kernels consume it by its device-side count.
-void run_gpu_stages_queued(BsfHandle* h, int n) {
+void run_gpu_stages_queued(BsfHandle* h, int n, bool timed = false);
+
+void record(BsfHandle* h, int i) { check(cudaEventRecord(h->ev[i], h->stream), "event"); }
+
+// Queued form: the screened Stage0 kernel appends P19 survivors to the device
+// coarse queue; the screened coarse kernels consume it by its device-side count.
+void run_gpu_stages_queued(BsfHandle* h, int n, bool timed) {
     check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
-    launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, h->dCoarseQueue, h->dCounters,
-                  h->capacity * h->centers, h->stream);
-    launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, LatticeBuffers{}, h->dSigns,
-                        h->dLabels, h->dStats, h->dRegions, h->centers, h->stream);
+    launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, h->dCoarseQueue, h->dCounters,
+                       h->capacity * h->centers, h->stream);
+    if (timed) record(h, 2);
+    launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->stream);
+    launch_coarse_cc(h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->dLabels, h->dStats, h->dRegions,
+                     h->centers, h->stream);
+    if (timed) record(h, 3);
     h->launches += 3;
 }
 
@@ -264,8 +273,6 @@ void run_gpu_stages(BsfHandle* h, int n) {
     else run_gpu_stages_queued(h, n);
 }
 
-void record(BsfHandle* h, int i) { check(cudaEventRecord(h->ev[i], h->stream), "event"); }
-
 // Stage0 and coarse bracketed by events (event 2 sits between them in the
 // queued form; in the plain form the host round trips fall inside stage 1/2).
 void run_gpu_stages_timed(BsfHandle* h, int n) {
@@ -275,14 +282,7 @@ void run_gpu_stages_timed(BsfHandle* h, int n) {
         record(h, 3);
         return;
     }
-    check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
-    launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, h->dCoarseQueue, h->dCounters,
-                  h->capacity * h->centers, h->stream);
-    record(h, 2);
-    launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, LatticeBuffers{}, h->dSigns,
-                        h->dLabels, h->dStats, h->dRegions, h->centers, h->stream);
-    record(h, 3);
-    h->launches += 3;
+    run_gpu_stages_queued(h, n, true);
 }
 
 void read_stage_times(BsfHandle* h) {
@@ -476,6 +476,8 @@ void* bsf_open(const bsf_config* cfgIn) {
         check(cudaSetDevice(cfg.device), "cudaSetDevice");
         check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
         init_lcg_tables();
+        init_stage0_fast();
+        init_coarse_fast();
         h->capacity = static_cast<int>(cfg.capacity);
         h->centers = cfg.centers;
         h->prof = profile_by_id(cfg.profile);
@@ -586,7 +588,10 @@ int bsf_p20_filter(void* hv, const int64_t* seeds, uint32_t count, uint8_t* out,
         // The P20 count of centre 0 comes out of the fused Stage0 kernel; the
         // stream protocol reports it for the world's first region only.
         check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
-        launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, nullptr, h->dCounters, 0, h->stream);
+        if (h->mode == BSF_MODE_PLAIN)
+            launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, nullptr, h->dCounters, 0, h->stream);
+        else
+            launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, nullptr, h->dCounters, 0, h->stream);
         k_pack_p20<<<(n + 255) / 256, 256, 0, h->stream>>>(h->dRegions, n, h->centers, h->dOut);
         h->launches += 2;
         check(cudaGetLastError(), "k_pack_p20");

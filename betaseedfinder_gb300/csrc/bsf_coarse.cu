@@ -368,6 +368,15 @@ void launch_coarse_score(const StateCache& cache, const RegionRef* dQueue, const
     check(cudaGetLastError(), "k_coarse_score");
 }
 
+void launch_coarse_cc(const RegionRef* dQueue, const int* dCount, int maxCount, std::uint32_t* dSignScratch,
+                      int* dLabelScratch, int* dStatScratch, RegionInfo* dRegions, int centers, cudaStream_t stream) {
+    if (maxCount <= 0) return;
+    int* err = dStatScratch + static_cast<std::size_t>(COARSE_SCORE_CTAS) * COARSE_CELLS * 2;
+    k_coarse_score<<<std::min(maxCount, COARSE_SCORE_CTAS), CC_THREADS, 0, stream>>>(
+        dSignScratch, dQueue, dCount, maxCount, dLabelScratch, dStatScratch, dRegions, centers, err);
+    check(cudaGetLastError(), "k_coarse_score");
+}
+
 void launch_lattice_noise(const StateCache& cache, const LatticeJob* dJobs, int jobs, int side,
                           const LatticeBuffers& buf, cudaStream_t stream) {
     if (jobs <= 0) return;

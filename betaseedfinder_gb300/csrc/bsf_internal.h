@@ -102,6 +102,17 @@ void launch_coarse_score(const StateCache& cache, const RegionRef* dQueue, const
                          const LatticeBuffers& buf, std::uint32_t* dSignScratch, int* dLabelScratch,
                          int* dStatScratch, RegionInfo* dRegions, int centers, cudaStream_t stream);
 std::size_t coarse_scratch_bytes_per_region();
+// Component score of coarse sign masks already in dSignScratch.
+void launch_coarse_cc(const RegionRef* dQueue, const int* dCount, int maxCount, std::uint32_t* dSignScratch,
+                      int* dLabelScratch, int* dStatScratch, RegionInfo* dRegions, int centers, cudaStream_t stream);
+
+// Screened (FP32 + exact fallback) kernels: identical outputs, far fewer FP64 operations.
+void init_stage0_fast();
+void launch_stage0_fast(const StateCache& cache, int n, int centers, const Profile& prof, RegionInfo* dRegions,
+                        RegionRef* dCoarseQueue, int* dCoarseCount, int coarseCapacity, cudaStream_t stream);
+void init_coarse_fast();
+void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
+                              std::uint32_t* dSigns, cudaStream_t stream);
 int coarse_score_ctas();  // label/stat scratch is per CTA of the persistent score grid
 
 // Exact scan of one region at one radius; result in *dIsland (device).

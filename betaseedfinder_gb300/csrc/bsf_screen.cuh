@@ -1,0 +1,359 @@
+// FP32 screening of lattice density signs with rigorous error bounds.
+//
+// GB300's FP64 pipe issues about 1.75 operations per clock per SM against 128
+// for FP32, and every output of this path is a function of density *signs*
+// (stage masks, coarse cells, block bitmaps). So the octave arithmetic runs in
+// FP32 from exact FP64 lattice coordinates, each result carries an upper bound
+// of its distance to the FP64 value the reference computes, and a sign is
+// accepted only when |value| exceeds that bound. Columns with any point inside
+// its bound are recomputed with the exact FP64 path (bsf_device.cuh), so the
+// decisions are bit-identical to the reference by construction.
+//
+// Error model (u = 2^-24, FP32 round-to-nearest, products with FMA rounded
+// once): inputs are FP64 values rounded to FP32 (error <= u|x|). For one 3D
+// octave value (corner gradients |g| <= 2, three lerp levels, all |.| <= 2):
+// gradient 2.4e-7, x-lerp 1.32e-6, y-lerp 4.56e-6, z-lerp 1.43e-5 -> E_OCT3 =
+// 2e-5. For one 2D octave value (two lerp levels): 4.6e-6 -> E_OCT2 = 6e-6.
+// Octave sums add w_o * E plus the running-sum rounding u * 2 * sum(w).
+// Everything after the octave sums is tracked per value with (value, bound)
+// pairs (struct Fe) whose operations add the propagated and rounding terms;
+// piecewise branches add their jump or mark the column ambiguous. The final
+// bound is doubled and gets an absolute 1e-6 for the FP64 side's own rounding.
+#pragma once
+
+#include "bsf_device.cuh"
+
+namespace bsf {
+namespace screen {
+
+constexpr float U = 5.9604645e-8f;  // 2^-24
+constexpr float E_OCT3 = 2.0e-5f;
+constexpr float E_OCT2 = 6.0e-6f;
+
+// Value with an upper bound of its absolute error against the FP64 reference.
+struct Fe {
+    float v, e;
+};
+
+__device__ __forceinline__ Fe fe_exact(double x) {
+    const float f = static_cast<float>(x);
+    return Fe{f, fabsf(f) * U};
+}
+__device__ __forceinline__ Fe fe_add(Fe a, Fe b) {
+    const float v = a.v + b.v;
+    return Fe{v, a.e + b.e + fabsf(v) * U};
+}
+__device__ __forceinline__ Fe fe_sub(Fe a, Fe b) {
+    const float v = a.v - b.v;
+    return Fe{v, a.e + b.e + fabsf(v) * U};
+}
+__device__ __forceinline__ Fe fe_mul(Fe a, Fe b) {
+    const float v = a.v * b.v;
+    return Fe{v, fabsf(a.v) * b.e + fabsf(b.v) * a.e + a.e * b.e + fabsf(v) * U};
+}
+__device__ __forceinline__ Fe fe_scale(Fe a, float c) {  // c exact in FP32
+    const float v = a.v * c;
+    return Fe{v, a.e * fabsf(c) + fabsf(v) * U};
+}
+// a / b for b bounded away from zero (b.e < |b.v|); returns a huge bound otherwise.
+__device__ __forceinline__ Fe fe_div(Fe a, Fe b) {
+    const float v = a.v / b.v;
+    const float den = fabsf(b.v) - b.e;
+    if (!(den > 0.0f)) return Fe{v, 3.0e38f};
+    return Fe{v, (a.e + fabsf(v) * b.e) / den + 2.0f * fabsf(v) * U};
+}
+__device__ __forceinline__ Fe fe_clamp_hi(Fe a, float hi) { return Fe{a.v > hi ? hi : a.v, a.e}; }
+__device__ __forceinline__ Fe fe_clamp_lo(Fe a, float lo) { return Fe{a.v < lo ? lo : a.v, a.e}; }
+
+// ---- lattice axis entries --------------------------------------------------
+// One coordinate of one octave: exact FP64 lattice index and fraction, stored
+// as FP32 fraction, FP32 (fraction - 1) and FP32 fade, each the rounding of the
+// exact FP64 value.
+struct AxisF {
+    float f, f1, fd;
+    int i;
+};
+
+__device__ __forceinline__ AxisF make_axis(double scaled, double offset) {
+    double v = scaled + offset;
+    const int fl = jfloor(v);
+    v -= static_cast<double>(fl);
+    AxisF a;
+    a.i = fl & 255;
+    a.f = static_cast<float>(v);
+    a.f1 = static_cast<float>(v - 1.0);
+    a.fd = static_cast<float>(fade(v));
+    return a;
+}
+
+// Y axis entry of one 3D octave in FP32: the cell-start fraction (and minus 1),
+// own fade, cell ordinal and lattice index.
+struct YF {
+    float cf, cf1, fd;
+    unsigned char yi, cell, pad0, pad1;
+};
+
+__device__ __forceinline__ void build_yf(const YEntry* y64, YF* out) {
+    for (int y = 0; y < 17; ++y) {
+        out[y].cf = static_cast<float>(y64[y].cellFrac);
+        out[y].cf1 = static_cast<float>(y64[y].cellFrac - 1.0);
+        out[y].fd = static_cast<float>(y64[y].fade);
+        out[y].yi = static_cast<unsigned char>(y64[y].yi);
+        out[y].cell = static_cast<unsigned char>(y64[y].cell);
+        out[y].pad0 = out[y].pad1 = 0;
+    }
+}
+
+__device__ __forceinline__ float grad3f(int hash, float x, float y, float z) {
+    const int h = hash & 15;
+    const float u = h < 8 ? x : y;
+    const float v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
+    return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+}
+
+__device__ __forceinline__ float lerpf(float t, float a, float b) { return __fmaf_rn(t, b - a, a); }
+
+// FP32 3D octave over levels [Y0, Y0+N): acc[k] (+)= w * value.
+template <int Y0, int N>
+__device__ __forceinline__ void octave3f(const std::uint8_t* p, const AxisF& ax, const AxisF& az, const YF* yt,
+                                         float w, float* acc, bool first) {
+    const int xp0 = P(p, ax.i);
+    const int xp1 = P(p, ax.i + 1);
+    int active = -1;
+    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const YF e = yt[Y0 + k];
+        if (e.cell != active) {
+            active = e.cell;
+            const int p0 = xp0 + e.yi;
+            const int p00 = P(p, p0) + az.i;
+            const int p01 = P(p, p0 + 1) + az.i;
+            const int p1 = xp1 + e.yi;
+            const int p10 = P(p, p1) + az.i;
+            const int p11 = P(p, p1 + 1) + az.i;
+            c00 = lerpf(ax.fd, grad3f(P(p, p00), ax.f, e.cf, az.f), grad3f(P(p, p10), ax.f1, e.cf, az.f));
+            c01 = lerpf(ax.fd, grad3f(P(p, p01), ax.f, e.cf1, az.f), grad3f(P(p, p11), ax.f1, e.cf1, az.f));
+            c10 = lerpf(ax.fd, grad3f(P(p, p00 + 1), ax.f, e.cf, az.f1), grad3f(P(p, p10 + 1), ax.f1, e.cf, az.f1));
+            c11 = lerpf(ax.fd, grad3f(P(p, p01 + 1), ax.f, e.cf1, az.f1), grad3f(P(p, p11 + 1), ax.f1, e.cf1, az.f1));
+        }
+        const float v = lerpf(az.fd, lerpf(e.fd, c00, c01), lerpf(e.fd, c10, c11)) * w;
+        acc[k] = first ? v : acc[k] + v;
+    }
+}
+
+// FP32 2D octave value (legacy 2D sampler, NoiseGeneratorPerlin173.java:188-223).
+__device__ __forceinline__ float octave2f(const std::uint8_t* p, const AxisF& ax, const AxisF& az) {
+    const int a0 = P(p, ax.i);
+    const int a1 = P(p, a0) + az.i;
+    const int b0 = P(p, ax.i + 1);
+    const int b1 = P(p, b0) + az.i;
+    // grad2_legacy in FP32: the signed-zero terms cannot change a value beyond its bound.
+    const int h = P(p, a1) & 15;
+    float g0;
+    switch (h) {
+        case 0: case 2: g0 = ax.f; break;
+        case 1: case 3: g0 = -ax.f; break;
+        case 4: g0 = ax.f + az.f; break;
+        case 5: g0 = -ax.f + az.f; break;
+        case 6: g0 = ax.f - az.f; break;
+        case 7: g0 = -ax.f - az.f; break;
+        case 8: case 9: case 13: g0 = az.f; break;
+        case 12: g0 = ax.f; break;
+        case 14: g0 = -ax.f; break;
+        default: g0 = -az.f; break;
+    }
+    const float q0 = lerpf(ax.fd, g0, grad3f(P(p, b1), ax.f1, 0.0f, az.f));
+    const float q1 = lerpf(ax.fd, grad3f(P(p, a1 + 1), ax.f, 0.0f, az.f1), grad3f(P(p, b1 + 1), ax.f1, 0.0f, az.f1));
+    return lerpf(az.fd, q0, q1);
+}
+
+// Bound of an octave sum: weights 2^0..2^(n-1), per-octave bound e, running
+// sum |S_k| <= 2 * (2^(k+1) - 1) rounded once per add.
+__host__ __device__ constexpr float octave_sum_bound(int n, float e) {
+    return static_cast<float>((1 << n) - 1) * e + U * 2.0f * static_cast<float>(1 << (n + 1));
+}
+constexpr float E_N2 = octave_sum_bound(16, E_OCT3);  // noise2 / noise3
+constexpr float E_N1 = octave_sum_bound(8, E_OCT3);   // noise1
+constexpr float E_N4 = octave_sum_bound(10, E_OCT2);  // noise4
+constexpr float E_N5 = octave_sum_bound(16, E_OCT2);  // noise5
+
+// Simplex sample with exact FP64 lattice geometry and an FP32 kernel: the
+// offsets d11..d16 are FP64 (they cancel large coordinates), the falloff and
+// gradients are FP32 tracked with bounds. Returns 70*(n0+n1+n2) with its bound.
+__device__ __forceinline__ float simplex_corner(float x, float z, int g, float& err) {
+    // x, z carry error <= u|.| (rounded exact offsets)
+    Fe X{x, fabsf(x) * U}, Z{z, fabsf(z) * U};
+    Fe t = fe_sub(fe_sub(Fe{0.5f, 0.0f}, fe_mul(X, X)), fe_mul(Z, Z));
+    if (fabsf(t.v) <= t.e) {
+        // the FP64 branch t < 0 may differ; the contribution is at most (|t|+e)^4 * 2
+        const float m = fabsf(t.v) + t.e;
+        err += m * m * m * m * 2.0f;
+        return 0.0f;
+    }
+    if (t.v < 0.0f) return 0.0f;
+    Fe gx, gz;
+    // simplexGrad2 (NoiseGenerator2173.java:61-75)
+    float gv;
+    switch (g) {
+        case 0: gv = x + z; gx = fe_add(X, Z); break;
+        case 1: gv = -x + z; gx = fe_sub(Z, X); break;
+        case 2: gv = x - z; gx = fe_sub(X, Z); break;
+        case 3: gv = -x - z; gx = fe_add(X, Z); gx.v = -gx.v; break;
+        case 4: case 6: gv = x; gx = X; break;
+        case 5: case 7: gv = -x; gx = Fe{-X.v, X.e}; break;
+        case 8: case 10: gv = z; gx = Z; break;
+        default: gv = -z; gx = Fe{-Z.v, Z.e}; break;
+    }
+    (void)gv;
+    (void)gz;
+    const Fe t2 = fe_mul(t, t);
+    const Fe t4 = fe_mul(t2, t2);
+    const Fe n = fe_mul(t4, gx);
+    err += n.e;
+    return n.v;
+}
+
+__device__ __forceinline__ Fe simplex2f(const Gen& s, double xs, double zs) {
+    constexpr double F = 0.3660254037844386;
+    constexpr double G = 0.21132486540518713;
+    const double d5 = xs + s.a;
+    const double d6 = zs + s.b;
+    const double d7 = (d5 + d6) * F;
+    const int j1 = simplex_floor(d5 + d7);
+    const int k1 = simplex_floor(d6 + d7);
+    const double d8 = static_cast<double>(j1 + k1) * G;
+    const double d11 = d5 - (static_cast<double>(j1) - d8);
+    const double d12 = d6 - (static_cast<double>(k1) - d8);
+    const int b0 = d11 > d12 ? 1 : 0;
+    const int b1 = d11 > d12 ? 0 : 1;
+    const double d13 = d11 - static_cast<double>(b0) + G;
+    const double d14 = d12 - static_cast<double>(b1) + G;
+    const double d15 = d11 - 1.0 + 2.0 * G;
+    const double d16 = d12 - 1.0 + 2.0 * G;
+    const int l1 = j1 & 255;
+    const int i2 = k1 & 255;
+    const int g0 = P(s.p, l1 + P(s.p, i2)) % 12;
+    const int g1 = P(s.p, l1 + b0 + P(s.p, i2 + b1)) % 12;
+    const int g2 = P(s.p, l1 + 1 + P(s.p, i2 + 1)) % 12;
+    float err = 0.0f;
+    const float n0 = simplex_corner(static_cast<float>(d11), static_cast<float>(d12), g0, err);
+    const float n1 = simplex_corner(static_cast<float>(d13), static_cast<float>(d14), g1, err);
+    const float n2 = simplex_corner(static_cast<float>(d15), static_cast<float>(d16), g2, err);
+    const float sum = n0 + n1 + n2;
+    const float v = 70.0f * sum;
+    return Fe{v, 70.0f * (err + 2.0f * fabsf(sum) * U) + fabsf(v) * U};
+}
+
+// Climate (temperature, rain) with bounds (WorldChunkManager173.java:95-126).
+__device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe& temperature, Fe& rain) {
+    const double X = static_cast<double>(bx);
+    const double Z = static_cast<double>(bz);
+    Fe raw[3];
+    const int base[3] = {0, 4, 8};
+    const int count[3] = {4, 4, 2};
+    const double scale[3] = {0.02500000037252903, 0.05000000074505806, 0.25};
+    const double octScale[3] = {0.25, 0.3333333333333333, 0.5882352941176471};
+#pragma unroll
+    for (int grp = 0; grp < 3; ++grp) {
+        const double d2 = scale[grp] / 1.5;
+        double d6 = 1.0;
+        double d7 = 1.0;
+        Fe acc{0.0f, 0.0f};
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            if (o < count[grp]) {
+                const double sx = d2 * d7;
+                const float w = static_cast<float>(0.55 / d6);  // 0.55 * 2^k: FP32 rounding of w tracked below
+                const Fe s = simplex2f(t(ST_TEMP + base[grp] + o), X * sx, Z * sx);
+                const Fe term{s.v * w, s.e * w + fabsf(s.v * w) * 2.0f * U};
+                acc = fe_add(acc, term);
+                d7 *= octScale[grp];
+                d6 *= 0.5;
+            }
+        }
+        raw[grp] = acc;
+    }
+    // Decimal constants are not exact in FP32: each carries its own rounding bound.
+    const Fe c11{1.1f, 1.1f * U}, c015{0.15f, 0.15f * U};
+    const Fe d0 = fe_add(fe_mul(raw[2], c11), Fe{0.5f, 0.0f});
+    Fe d3 = fe_add(fe_mul(fe_add(fe_mul(raw[0], c015), Fe{0.7f, 0.7f * U}), Fe{0.99f, 0.99f * U}),
+                   fe_mul(d0, Fe{0.01f, 0.01f * U}));
+    Fe d4 = fe_add(fe_mul(fe_add(fe_mul(raw[1], c015), Fe{0.5f, 0.0f}), Fe{0.998f, 0.998f * U}),
+                   fe_mul(d0, Fe{0.002f, 0.002f * U}));
+    const Fe om = fe_sub(Fe{1.0f, 0.0f}, d3);
+    d3 = fe_sub(Fe{1.0f, 0.0f}, fe_mul(om, om));
+    d3 = fe_clamp_hi(fe_clamp_lo(d3, 0.0f), 1.0f);
+    d4 = fe_clamp_hi(fe_clamp_lo(d4, 0.0f), 1.0f);
+    temperature = d3;
+    rain = d4;
+}
+
+// Column shape with bounds (BetaTerrain173.java:753-804). Returns false when
+// the d6 < 0 branch (which zeroes d5) cannot be decided within the bound.
+__device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, Fe& d5out, Fe& d7out) {
+    const Fe d3 = fe_mul(rain, temp);
+    Fe d4 = fe_sub(Fe{1.0f, 0.0f}, d3);
+    d4 = fe_mul(d4, d4);
+    d4 = fe_mul(d4, d4);
+    d4 = fe_sub(Fe{1.0f, 0.0f}, d4);
+    Fe d5 = fe_scale(fe_add(n4, Fe{256.0f, 0.0f}), 1.0f / 512.0f);
+    d5 = fe_clamp_hi(fe_mul(d5, d4), 1.0f);
+    Fe d6 = fe_div(n5, Fe{8000.0f, 0.0f});
+    if (fabsf(d6.v) <= d6.e) {
+        d6 = Fe{fabsf(d6.v), d6.e};  // -d6*0.3 and d6 agree at 0: Lipschitz 1
+    } else if (d6.v < 0.0f) {
+        d6 = fe_scale(Fe{-d6.v, d6.e}, 1.0f);
+        d6 = fe_mul(d6, Fe{0.3f, 0.3f * U});
+    }
+    d6 = fe_sub(fe_scale(d6, 3.0f), Fe{2.0f, 0.0f});
+    if (fabsf(d6.v) <= d6.e) return false;  // d5 = 0 branch undecidable
+    if (d6.v < 0.0f) {
+        d6 = fe_scale(d6, 0.5f);
+        d6 = fe_clamp_lo(d6, -1.0f);
+        d6 = fe_div(d6, Fe{1.4f, 1.4f * U});
+        d6 = fe_scale(d6, 0.5f);
+        d5 = Fe{0.0f, 0.0f};
+    } else {
+        d6 = fe_clamp_hi(d6, 1.0f);
+        d6 = fe_scale(d6, 0.125f);
+    }
+    d5 = fe_clamp_lo(d5, 0.0f);
+    d5 = fe_add(d5, Fe{0.5f, 0.0f});
+    d6 = fe_scale(fe_scale(d6, 17.0f), 1.0f / 16.0f);
+    d5out = d5;
+    d7out = fe_add(Fe{8.5f, 0.0f}, fe_scale(d6, 4.0f));
+    return true;
+}
+
+// Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1
+// when decided, 0 when the FP64 value could have either sign.
+__device__ __forceinline__ int density_sign_f(int y, Fe d5, Fe d7, float n1, float n2, float n3) {
+    const Fe d10{n2 * (1.0f / 512.0f), E_N2 / 512.0f + fabsf(n2) * (U / 512.0f)};
+    const Fe d11{n3 * (1.0f / 512.0f), E_N2 / 512.0f + fabsf(n3) * (U / 512.0f)};
+    const Fe d12 = fe_scale(fe_add(fe_div(Fe{n1, E_N1}, Fe{10.0f, 0.0f}), Fe{1.0f, 0.0f}), 0.5f);
+    Fe d8;
+    if (d12.v + d12.e < 0.0f) {
+        d8 = d10;
+    } else if (d12.v - d12.e > 1.0f) {
+        d8 = d11;
+    } else {
+        // interior (or a clamp edge): the lerp with t clamped to [0, 1] covers both sides
+        const Fe t = fe_clamp_hi(fe_clamp_lo(d12, 0.0f), 1.0f);
+        d8 = fe_add(d10, fe_mul(fe_sub(d11, d10), t));
+    }
+    Fe d9 = fe_div(fe_scale(fe_sub(Fe{static_cast<float>(y), 0.0f}, d7), 12.0f), d5);
+    if (d9.v < 0.0f || fabsf(d9.v) <= d9.e) d9 = Fe{d9.v < 0.0f ? d9.v * 4.0f : d9.v, d9.e * 4.0f};
+    Fe d = fe_sub(d8, d9);
+    if (y > 13) {
+        const float d13 = static_cast<float>(y - 13) / 3.0f;  // exact as the reference's float division
+        d = fe_add(fe_mul(d, Fe{1.0f - d13, 2.0f * U}), Fe{-10.0f * d13, 20.0f * U});
+    }
+    const float bound = 2.0f * d.e + 1.0e-6f;
+    if (d.v > bound) return 1;
+    if (d.v < -bound) return -1;
+    return 0;
+}
+
+}  // namespace screen
+}  // namespace bsf
