@@ -148,6 +148,24 @@ uint64_t bsf_kernel_launches(const void* h);
  * includes its round trips). */
 int bsf_last_stage_ms(const void* h, float* ms4);
 
+/* Allocation-free variant of bsf_chunk_bitmaps. It has no counterpart in the
+ * reference: it exists for callers that cannot allocate GPU memory (a host
+ * that owns all device memory and passes in pre-allocated buffers, a serving
+ * loop where cudaMalloc would synchronise the device, a fixed memory budget).
+ * Inputs and outputs are caller-owned device buffers (d_seeds: count int64,
+ * d_bitmaps: count * 4096 bytes, d_hashes: count uint64) and the work is
+ * enqueued on `stream` (a cudaStream_t, NULL = default stream) without a
+ * synchronisation. Its scratch is a fixed array of BSF_NOALLOC_MAX_WORLDS
+ * generator caches (5.6 MB) compiled into the library, which every GPU that
+ * loads the library keeps until the process exits; count beyond the maximum
+ * returns BSF_E_LIMIT. The first call on each device does a one-time set-up
+ * (constant tables, the scratch address) and should come before any stream
+ * capture. All calls share the one array: calls whose work overlaps on the
+ * GPU race. err (optional, err_len bytes) receives a message on failure. */
+#define BSF_NOALLOC_MAX_WORLDS 256u
+int bsf_chunk_bitmaps_noalloc(const int64_t* d_seeds, uint32_t count, int32_t chunk_x, int32_t chunk_z,
+                              uint8_t* d_bitmaps, uint64_t* d_hashes, void* stream, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
