@@ -62,7 +62,8 @@ class MegaRecord(ctypes.Structure):
 class StageCounts(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "worlds", "regions", "p20_passed", "upper_passed", "high_passed", "p19_passed",
-        "mega_rejected", "coarse_evaluated", "coarse_passed", "islands", "rng_fallbacks", "lower_columns")]
+        "mega_rejected", "coarse_evaluated", "coarse_passed", "islands", "rng_fallbacks", "lower_columns",
+        "screened_tasks", "fallback_tasks")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -71,7 +72,8 @@ class StageCounts(ctypes.Structure):
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
-           "bsf_kernel_launches", "bsf_last_stage_ms"]
+           "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
+           "bsf_autotune", "bsf_set_launch_variants"]
 
 _lib = None
 
@@ -111,8 +113,19 @@ def load(path=LIB_PATH):
     L.bsf_kernel_launches.argtypes = [vp]
     L.bsf_kernel_launches.restype = ctypes.c_uint64
     L.bsf_last_stage_ms.argtypes = [vp, P(ctypes.c_float)]
+    L.bsf_measure_peaks.argtypes = [P(ctypes.c_double)]
+    L.bsf_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]
+    L.bsf_set_launch_variants.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
     _lib = L
     return L
+
+
+def measure_peaks():
+    """Measured scalar issue rates of the current GPU: (FP64 adds/s, FP32 adds/s)."""
+    ops = (ctypes.c_double * 2)()
+    if load().bsf_measure_peaks(ops) != 0:
+        raise BsfError("bsf_measure_peaks failed")
+    return ops[0], ops[1]
 
 
 def default_match_settings(**overrides):
@@ -177,6 +190,15 @@ class Worker:
     @property
     def kernel_launches(self):
         return int(load().bsf_kernel_launches(self._h))
+
+    def autotune(self, worlds=4096):
+        """Pick the fastest launch shape of the screened kernels; returns the timing report."""
+        buf = ctypes.create_string_buffer(512)
+        self._check(load().bsf_autotune(self._h, worlds, buf, 512))
+        return buf.value.decode()
+
+    def set_launch_variants(self, stage0_variant, coarse_variant):
+        self._check(load().bsf_set_launch_variants(self._h, stage0_variant, coarse_variant))
 
     def last_stage_ms(self):
         """Per-stage device times of the last batch: setup, Stage0+P19, coarse, exact (ms)."""

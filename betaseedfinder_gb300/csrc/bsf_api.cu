@@ -105,6 +105,17 @@ __global__ void k_stage_counts(const RegionInfo* __restrict__ regions, int count
     }
 }
 
+// Issue-rate probes: 8 independent dependent-add chains per thread.
+template <typename T>
+__global__ void k_add_chains(T* out, int iters, T inc) {
+    T a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        a0 += inc; a1 += inc; a2 += inc; a3 += inc; a4 += inc; a5 += inc; a6 += inc; a7 += inc;
+    }
+    const T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == static_cast<T>(-1)) out[0] = s;  // keeps the chains alive
+}
+
 }  // namespace
 }  // namespace bsf
 
@@ -137,6 +148,7 @@ struct BsfHandle {
     RegionRef* dExactQueue = nullptr;
     void* dExactBase = nullptr;
     ExactScratch exact;
+    Stage0FastScratch fs;
     Island* dIsland = nullptr;
     int* dPrevMin = nullptr;
     int* dPrevMax = nullptr;
@@ -147,6 +159,18 @@ struct BsfHandle {
     std::vector<RegionInfo> hRegions;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stageMs[4] = {0, 0, 0, 0};
+    unsigned long long* hPinned = nullptr;  // stage counters [0..7], screen stats [8..11], counters [12..13]
+    struct CachedGraph {
+        cudaGraphExec_t exec;
+        cudaStream_t stream;
+        int variants;  // launch-shape variants the graph was captured with
+    };
+    std::vector<std::pair<long long, CachedGraph>> graphs;  // batch graphs by (worlds, seed source)
+
+    void drop_graphs() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second.exec);
+        graphs.clear();
+    }
 
     void alloc(void** p, std::size_t bytes, const char* what) { check(cudaMalloc(p, bytes), what); }
 };
@@ -220,20 +244,30 @@ void stage_seeds(BsfHandle* h, const std::int64_t* seeds, int n, bool hostSeeds)
 // queue; the coarse kernels consume it by its device-side count.
 void run_gpu_stages_queued(BsfHandle* h, int n, bool timed = false);
 
-void record(BsfHandle* h, int i) { check(cudaEventRecord(h->ev[i], h->stream), "event"); }
+// External event records: under stream capture they become event-record nodes
+// of the batch graph, so replays still time every stage.
+void record(BsfHandle* h, int i) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    check(cudaStreamIsCapturing(h->stream, &st), "capture status");
+    if (st == cudaStreamCaptureStatusActive)
+        check(cudaEventRecordWithFlags(h->ev[i], h->stream, cudaEventRecordExternal), "event");
+    else
+        check(cudaEventRecord(h->ev[i], h->stream), "event");
+}
 
 // Queued form: the screened Stage0 kernel appends P19 survivors to the device
 // coarse queue; the screened coarse kernels consume it by its device-side count.
 void run_gpu_stages_queued(BsfHandle* h, int n, bool timed) {
     check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
     launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, h->dCoarseQueue, h->dCounters,
-                       h->capacity * h->centers, h->stream);
+                       h->capacity * h->centers, h->fs, h->stream);
     if (timed) record(h, 2);
-    launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->stream);
+    launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->fs.stats,
+                             h->stream);
     launch_coarse_cc(h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->dLabels, h->dStats, h->dRegions,
                      h->centers, h->stream);
     if (timed) record(h, 3);
-    h->launches += 3;
+    h->launches += 4;
 }
 
 // Plain form: stage by stage with a host round trip after each; the host
@@ -349,6 +383,73 @@ Island resolve(BsfHandle* h, int world, int ccx, int ccz, int radius, int coarse
     return match;
 }
 
+// The GPU part of one batch, all on h->stream and free of host-side work, so it
+// can be captured into a graph: seed upload (seedSource 2: from the handle's
+// pinned staging; 1: from host `seeds` via the staging; 0: already in dSeeds
+// or given as device `seeds`), generator setup, stages, stage counters and the
+// download of the counters into pinned host memory.
+void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seeds) {
+    check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
+    check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
+    check(cudaMemsetAsync(h->fs.stats, 0, 4 * sizeof(unsigned long long), h->stream), "memset");
+    record(h, 0);
+    if (seedSource == 2) {
+        check(cudaMemcpyAsync(h->dSeeds, h->hSeeds, static_cast<std::size_t>(n) * 8, cudaMemcpyHostToDevice,
+                              h->stream), "seed upload");
+        launch_world_init(h->dSeeds, n, h->cache, h->dCounters + 1, h->stream);
+        ++h->launches;
+    } else if (seedSource == 1) {
+        stage_seeds(h, seeds, n, true);
+    } else {
+        launch_world_init(seeds ? seeds : h->dSeeds, n, h->cache, h->dCounters + 1, h->stream);
+        ++h->launches;
+    }
+    record(h, 1);
+    run_gpu_stages_timed(h, n);
+    const int regions = n * h->centers;
+    k_stage_counts<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, h->prof, h->dStageCounts,
+                                                                h->dExactQueue, h->dCounters + 2, h->exactCap,
+                                                                h->centers);
+    ++h->launches;
+    check(cudaGetLastError(), "k_stage_counts");
+    check(cudaMemcpyAsync(h->hPinned, h->dStageCounts, 8 * 8, cudaMemcpyDeviceToHost, h->stream), "counts");
+    check(cudaMemcpyAsync(h->hPinned + 8, h->fs.stats, 4 * 8, cudaMemcpyDeviceToHost, h->stream), "screen stats");
+    check(cudaMemcpyAsync(h->hPinned + 12, h->dCounters, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+          "counts");
+}
+
+// Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters.
+constexpr int kBatchGraphKernels = 6;
+
+cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
+    const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
+    const int variants = get_stage0_fast_variant() * 64 + get_coarse_fast_variant();
+    for (const auto& g : h->graphs)
+        if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
+    const unsigned long long launchesBefore = h->launches;
+    cudaGraph_t graph = nullptr;
+    check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    try {
+        enqueue_batch(h, n, hostSeeds ? 2 : 0, nullptr);
+    } catch (...) {
+        cudaStreamEndCapture(h->stream, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        throw;
+    }
+    check(cudaStreamEndCapture(h->stream, &graph), "graph capture");
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t rc = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    check(rc, "graph instantiate");
+    h->launches = launchesBefore;  // capture issued nothing; replays are counted per launch
+    if (h->graphs.size() >= 8) {
+        cudaGraphExecDestroy(h->graphs.front().second.exec);
+        h->graphs.erase(h->graphs.begin());
+    }
+    h->graphs.push_back({key, BsfHandle::CachedGraph{exec, h->stream, variants}});
+    return exec;
+}
+
 int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, uint32_t count,
                int32_t radius, const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
                uint32_t* recordsCount, bsf_stage_counts* counts) {
@@ -359,22 +460,21 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     cudaStream_t saved = h->stream;
     if (userStream) h->stream = userStream;
     const int n = static_cast<int>(count);
-    check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
-    check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
-    record(h, 0);
-    stage_seeds(h, seeds, n, hostSeeds);
-    record(h, 1);
-    run_gpu_stages_timed(h, n);
     const int regions = n * h->centers;
-    k_stage_counts<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, h->prof, h->dStageCounts,
-                                                                h->dExactQueue, h->dCounters + 2, h->exactCap,
-                                                                h->centers);
-    ++h->launches;
-    check(cudaGetLastError(), "k_stage_counts");
-    unsigned long long hc[8];
-    int hcount[4];
-    check(cudaMemcpyAsync(hc, h->dStageCounts, sizeof(hc), cudaMemcpyDeviceToHost, h->stream), "counts");
-    check(cudaMemcpyAsync(hcount, h->dCounters, sizeof(hcount), cudaMemcpyDeviceToHost, h->stream), "counts");
+    if (h->mode == BSF_MODE_QUEUED) {
+        // Queued form: one CUDA graph per (batch size, seed source) replays the
+        // whole GPU part of the batch; the seeds reach the handle's buffers first.
+        if (hostSeeds) std::memcpy(h->hSeeds, seeds, static_cast<std::size_t>(n) * 8);
+        else check(cudaMemcpyAsync(h->dSeeds, seeds, static_cast<std::size_t>(n) * 8, cudaMemcpyDeviceToDevice,
+                                   h->stream), "seed copy");
+        check(cudaGraphLaunch(batch_graph(h, n, hostSeeds), h->stream), "batch graph");
+        h->launches += kBatchGraphKernels;
+    } else {
+        enqueue_batch(h, n, hostSeeds ? 1 : 0, seeds);
+    }
+    unsigned long long* hc = h->hPinned;
+    unsigned long long* hs = h->hPinned + 8;
+    const int* hcount = reinterpret_cast<const int*>(h->hPinned + 12);
     check(cudaStreamSynchronize(h->stream), "mega batch");
     if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
     read_stage_times(h);
@@ -431,6 +531,8 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
         counts->islands = islands;
         counts->rng_fallbacks = static_cast<uint64_t>(hcount[1]);
         counts->lower_columns = hc[7];
+        counts->screened_tasks = h->mode == BSF_MODE_PLAIN ? 0 : hs[0] + hs[2];
+        counts->fallback_tasks = h->mode == BSF_MODE_PLAIN ? 0 : hs[1] + hs[3];
     }
     h->stream = saved;
     return BSF_OK;
@@ -502,6 +604,12 @@ void* bsf_open(const bsf_config* cfgIn) {
         h->alloc(reinterpret_cast<void**>(&h->dHashes), n * 8, "hashes");
         h->alloc(reinterpret_cast<void**>(&h->dStageCounts), 8 * sizeof(unsigned long long), "stage counts");
         h->alloc(reinterpret_cast<void**>(&h->dExactQueue), h->exactCap * sizeof(RegionRef), "exact queue");
+        h->fs.p19Capacity = static_cast<int>(regions);
+        h->alloc(reinterpret_cast<void**>(&h->fs.p19Queue), regions * sizeof(RegionRef), "p19 queue");
+        h->alloc(reinterpret_cast<void**>(&h->fs.highest), regions * 256, "p19 grids");
+        h->alloc(reinterpret_cast<void**>(&h->fs.p19Count), 64, "p19 count");
+        h->alloc(reinterpret_cast<void**>(&h->fs.stats), 8 * sizeof(unsigned long long), "screen stats");
+        check(cudaMemset(h->fs.stats, 0, 8 * sizeof(unsigned long long)), "memset");
         const std::size_t eb = exact_scratch_bytes(cfg.max_exact_radius);
         h->alloc(&h->dExactBase, eb, "exact scratch");
         exact_scratch_carve(h->exact, h->dExactBase, cfg.max_exact_radius);
@@ -512,6 +620,7 @@ void* bsf_open(const bsf_config* cfgIn) {
         h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
         for (auto& e : h->ev) check(cudaEventCreate(&e), "event");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hSeeds), n * 8), "pinned seeds");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hPinned), 16 * sizeof(unsigned long long)), "pinned counters");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
               "pinned output");
         check(cudaDeviceSynchronize(), "open");
@@ -527,15 +636,18 @@ void bsf_close(void* hv) {
     BsfHandle* h = static_cast<BsfHandle*>(hv);
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    h->drop_graphs();
     void* dev[] = {h->dSeeds, h->cache.perms, h->cache.offsets, h->dRegions, h->dCoarseQueue, h->dCounters,
                    h->dSigns, h->dLabels, h->dStats, h->dOut, h->dHashes, h->dStageCounts, h->dExactQueue,
-                   h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax};
+                   h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax, h->fs.p19Queue, h->fs.highest,
+                   h->fs.p19Count, h->fs.stats};
     for (void* p : dev)
         if (p) cudaFree(p);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
     if (h->hSeeds) cudaFreeHost(h->hSeeds);
     if (h->hOut) cudaFreeHost(h->hOut);
+    if (h->hPinned) cudaFreeHost(h->hPinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -591,7 +703,8 @@ int bsf_p20_filter(void* hv, const int64_t* seeds, uint32_t count, uint8_t* out,
         if (h->mode == BSF_MODE_PLAIN)
             launch_stage0(h->cache, n, h->centers, h->prof, nullptr, h->dRegions, nullptr, h->dCounters, 0, h->stream);
         else
-            launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, nullptr, h->dCounters, 0, h->stream);
+            launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, nullptr, h->dCounters, 0, h->fs,
+                               h->stream);
         k_pack_p20<<<(n + 255) / 256, 256, 0, h->stream>>>(h->dRegions, n, h->centers, h->dOut);
         h->launches += 2;
         check(cudaGetLastError(), "k_pack_p20");
@@ -685,6 +798,112 @@ int bsf_last_stage_ms(const void* hv, float* ms4) {
     if (!h || !ms4) return BSF_E_ARG;
     for (int i = 0; i < 4; ++i) ms4[i] = h->stageMs[i];
     return BSF_OK;
+}
+
+int bsf_autotune(void* hv, uint32_t worlds, char* report, size_t reportLen) {
+    return guarded(hv, [&](BsfHandle* h) {
+        const int n = static_cast<int>(std::min<uint32_t>(std::max<uint32_t>(worlds, 64u), h->capacity));
+        std::vector<std::int64_t> seeds(n);
+        for (int i = 0; i < n; ++i) seeds[i] = 0x5DEECE66DLL * 7919 + i;  // fixed calibration range
+        std::string rep;
+        char buf[96];
+        cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
+        stage_seeds(h, seeds.data(), n, true);
+        auto time_it = [&](auto&& fn) {
+            fn();  // warm-up (module load, caches)
+            check(cudaEventRecord(e0, h->stream), "event");
+            fn();
+            check(cudaEventRecord(e1, h->stream), "event");
+            check(cudaEventSynchronize(e1), "autotune");
+            float ms = 0.0f;
+            check(cudaEventElapsedTime(&ms, e0, e1), "event");
+            return ms;
+        };
+        auto stage0 = [&]() {
+            check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
+            launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, h->dCoarseQueue, h->dCounters,
+                               h->capacity * h->centers, h->fs, h->stream);
+        };
+        int best = 0;
+        float bestMs = 1e30f;
+        rep += "stage0:";
+        for (int v = 0; v < stage0_fast_variants(); ++v) {
+            set_stage0_fast_variant(v);
+            const float ms = time_it(stage0);
+            std::snprintf(buf, sizeof(buf), " %s=%.2fms", stage0_fast_variant_name(v), ms);
+            rep += buf;
+            if (ms < bestMs) { bestMs = ms; best = v; }
+        }
+        set_stage0_fast_variant(best);
+        rep += std::string(" -> ") + stage0_fast_variant_name(best) + "; coarse:";
+        stage0();  // leaves the coarse queue of the calibration batch on the device
+        best = 0;
+        bestMs = 1e30f;
+        for (int v = 0; v < coarse_fast_variants(); ++v) {
+            set_coarse_fast_variant(v);
+            const float ms = time_it([&]() {
+                launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, nullptr,
+                                         h->stream);
+            });
+            std::snprintf(buf, sizeof(buf), " %s=%.2fms", coarse_fast_variant_name(v), ms);
+            rep += buf;
+            if (ms < bestMs) { bestMs = ms; best = v; }
+        }
+        set_coarse_fast_variant(best);
+        rep += std::string(" -> ") + coarse_fast_variant_name(best);
+        check(cudaStreamSynchronize(h->stream), "autotune");
+        if (report && reportLen) {
+            std::strncpy(report, rep.c_str(), reportLen - 1);
+            report[reportLen - 1] = '\0';
+        }
+        return BSF_OK;
+    });
+}
+
+int bsf_set_launch_variants(void* hv, int32_t s0, int32_t co) {
+    return guarded(hv, [&](BsfHandle*) {
+        if (s0 < 0 || s0 >= stage0_fast_variants() || co < 0 || co >= coarse_fast_variants())
+            throw std::invalid_argument("bsf_set_launch_variants: variant index out of range");
+        set_stage0_fast_variant(s0);
+        set_coarse_fast_variant(co);
+        return BSF_OK;
+    });
+}
+
+int bsf_measure_peaks(double* ops) {
+    if (!ops) return BSF_E_ARG;
+    try {
+        int dev = 0, sms = 0;
+        check(cudaGetDevice(&dev), "device");
+        check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+        void* out = nullptr;
+        check(cudaMalloc(&out, 64), "probe buffer");
+        cudaEvent_t e0, e1;
+        check(cudaEventCreate(&e0), "event");
+        check(cudaEventCreate(&e1), "event");
+        const int blocks = sms * 8, threads = 256;
+        for (int kind = 0; kind < 2; ++kind) {
+            const int iters = kind == 0 ? 4096 : 262144;
+            float best = 1e30f;
+            for (int rep = 0; rep < 4; ++rep) {
+                check(cudaEventRecord(e0), "event");
+                if (kind == 0) k_add_chains<double><<<blocks, threads>>>(static_cast<double*>(out), iters, 1e-9);
+                else k_add_chains<float><<<blocks, threads>>>(static_cast<float*>(out), iters, 1e-9f);
+                check(cudaEventRecord(e1), "event");
+                check(cudaEventSynchronize(e1), "probe");
+                float ms = 0;
+                check(cudaEventElapsedTime(&ms, e0, e1), "event");
+                if (rep > 0 && ms < best) best = ms;
+            }
+            ops[kind] = static_cast<double>(blocks) * threads * 8.0 * iters / (best / 1e3);
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(out);
+        return BSF_OK;
+    } catch (const std::exception&) {
+        return BSF_E_CUDA;
+    }
 }
 
 uint64_t bsf_kernel_launches(const void* hv) {

@@ -1,13 +1,14 @@
 // Screened coarse 61x61x17 lattice signs for sm_103a.
 //
-// Persistent grid, one 512-thread CTA per SM looping over the queued regions.
-// Per region the CTA stages the world's generators, the 40 3D Y axes (FP64 and
-// FP32) and an axis table of the region's 61 X and 61 Z coarse coordinates for
-// the 66 lattice octaves (exact FP64 index / fraction / fade, stored in FP32).
-// Columns are processed in tiles of 512: the column shape (climate + noise4/5)
-// and then the three Y ranges of the 40 3D octaves, all in FP32 with error
-// bounds (bsf_screen.cuh). Undecided columns are recomputed in exact FP64, so
-// the 17-bit sign masks equal those of the exact coarse kernel bit for bit.
+// Persistent grid, two 256-thread CTAs per SM, looping over half-regions
+// (X rows 0..30 and 31..60 of each queued region). Per half-region the CTA
+// stages the world's generators, the 40 3D Y axes (FP32 and FP64) and an axis
+// table of its 31 X and 61 Z coarse coordinates for the 66 lattice octaves
+// (exact FP64 index / fraction / fade, stored as FP32). Columns are processed
+// in tiles of 256: column shape (climate at block 4c+2 + noise4/5), then the
+// three Y ranges of the 40 3D octaves, all in FP32 with error bounds
+// (bsf_screen.cuh). Undecided columns are recomputed in exact FP64, so the
+// 17-bit sign masks equal those of the FP64 coarse kernel bit for bit.
 #include "bsf_device.cuh"
 #include "bsf_internal.h"
 #include "bsf_screen.cuh"
@@ -20,28 +21,29 @@ namespace {
 
 using namespace screen;
 
-constexpr int CT = 512;
 constexpr int SIDE = 61;
 constexpr int COLS = SIDE * SIDE;
+constexpr int HALF_ROWS = 31;  // X rows of the first half; the second has 30
 constexpr int NOCT = 66;
-constexpr int TILE = 512;
-constexpr int FB_CAP = 1024;
+constexpr int MAX_TILE = 512;  // a tile is one column per thread of the CTA
+constexpr int FB_CAP = 256;
 
-struct AxisS {
-    float f, fd;
-    int i;
+struct Y64 {
+    double cellFrac, fade;
 };
 
 struct CoarseSmem {
     std::uint8_t perm[ST_COUNT * PERM_BYTES];
     double off[ST_COUNT][3];
-    YEntry y64[OCT3][17];
     YF yf[OCT3][17];
-    AxisS axis[NOCT][2][SIDE];
-    float shape[TILE][4];
-    std::uint32_t mask[TILE];
-    std::uint32_t fb[FB_CAP];
-    int fbCount;
+    Y64 y64[OCT3][17];
+    float xf[NOCT][HALF_ROWS], xd[NOCT][HALF_ROWS];
+    float zf[NOCT][SIDE], zd[NOCT][SIDE];
+    std::uint8_t xi[NOCT][HALF_ROWS], zi[NOCT][SIDE];
+    float shape[MAX_TILE][4];
+    std::uint32_t mask[MAX_TILE];
+    std::uint16_t fb[FB_CAP];
+    int fbCount, screened, fallbacks;
 };
 
 __device__ __forceinline__ GenTable gtab(const CoarseSmem& s) {
@@ -59,30 +61,41 @@ __device__ __forceinline__ double octave_scale(int o) {
     return 200.0 / static_cast<double>(1 << (o - 50));
 }
 
-__device__ __forceinline__ AxisF axf(const AxisS& a) { return AxisF{a.f, a.f - 1.0f, a.fd, a.i}; }
+__device__ __forceinline__ AxisF ax_x(const CoarseSmem& s, int o, int k) {
+    const float f = s.xf[o][k];
+    return AxisF{f, f - 1.0f, s.xd[o][k], s.xi[o][k]};
+}
+__device__ __forceinline__ AxisF ax_z(const CoarseSmem& s, int o, int k) {
+    const float f = s.zf[o][k];
+    return AxisF{f, f - 1.0f, s.zd[o][k], s.zi[o][k]};
+}
+
+template <int Y0, int N>
+__device__ void exact_octaves(const CoarseSmem& s, int base, int ycol, double sc0, double X, double Z, int count,
+                              double* acc) {
+    const GenTable t = gtab(s);
+    double amp = 1.0;
+    for (int o = 0; o < count; ++o) {
+        const double sc = sc0 * amp;
+        YEntry ya[17];
+        for (int k = 0; k < N; ++k) {
+            const int y = Y0 + k;
+            ya[y].cellFrac = s.y64[ycol + o][y].cellFrac;
+            ya[y].fade = s.y64[ycol + o][y].fade;
+            ya[y].yi = s.yf[ycol + o][y].yi;
+            ya[y].cell = s.yf[ycol + o][y].cell;
+        }
+        octave3_column<Y0, N>(t(base + o), X * sc, Z * sc, ya, 1.0 / amp, acc, o == 0);
+        amp /= 2.0;
+    }
+}
 
 template <int Y0, int N>
 __device__ unsigned exact_bits(const CoarseSmem& s, double X, double Z, double d5, double d7) {
-    const GenTable t = gtab(s);
     double a1[N], a2[N], a3[N];
-    double amp = 1.0;
-    for (int o = 0; o < 16; ++o) {
-        const double sc = NOISE_XZ * amp;
-        octave3_column<Y0, N>(t(ST_N2 + o), X * sc, Z * sc, s.y64[o], 1.0 / amp, a2, o == 0);
-        amp /= 2.0;
-    }
-    amp = 1.0;
-    for (int o = 0; o < 16; ++o) {
-        const double sc = NOISE_XZ * amp;
-        octave3_column<Y0, N>(t(ST_N3 + o), X * sc, Z * sc, s.y64[16 + o], 1.0 / amp, a3, o == 0);
-        amp /= 2.0;
-    }
-    amp = 1.0;
-    for (int o = 0; o < 8; ++o) {
-        const double sc = (NOISE_XZ / 80.0) * amp;
-        octave3_column<Y0, N>(t(ST_N1 + o), X * sc, Z * sc, s.y64[32 + o], 1.0 / amp, a1, o == 0);
-        amp /= 2.0;
-    }
+    exact_octaves<Y0, N>(s, ST_N2, 0, NOISE_XZ, X, Z, 16, a2);
+    exact_octaves<Y0, N>(s, ST_N3, 16, NOISE_XZ, X, Z, 16, a3);
+    exact_octaves<Y0, N>(s, ST_N1, 32, NOISE_XZ / 80.0, X, Z, 8, a1);
     unsigned bits = 0;
 #pragma unroll
     for (int k = 0; k < N; ++k)
@@ -118,22 +131,21 @@ __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int c
     return exact_bits<12, 5>(s, X, Z, d5, d7);
 }
 
-// Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds.
-__device__ __noinline__ void coarse_shape(CoarseSmem& s, int originX, int originZ, int kx, int kz, float* sh) {
-    const int cx = originX + kx, cz = originZ + kz;
+// Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds; kx is the half-local row.
+__device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
     Fe temp, rain;
     climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
     float n4 = 0.0f, n5 = 0.0f;
 #pragma unroll
     for (int o = 0; o < 10; ++o) {
-        const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, axf(s.axis[ST_N4 + o][0][kx]),
-                                 axf(s.axis[ST_N4 + o][1][kz])) * static_cast<float>(1 << o);
+        const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx), ax_z(s, ST_N4 + o, kz)) *
+                        static_cast<float>(1 << o);
         n4 = o == 0 ? v : n4 + v;
     }
 #pragma unroll
     for (int o = 0; o < 16; ++o) {
-        const float v = octave2f(s.perm + (ST_N5 + o) * PERM_BYTES, axf(s.axis[ST_N5 + o][0][kx]),
-                                 axf(s.axis[ST_N5 + o][1][kz])) * static_cast<float>(1 << o);
+        const float v = octave2f(s.perm + (ST_N5 + o) * PERM_BYTES, ax_x(s, ST_N5 + o, kx), ax_z(s, ST_N5 + o, kz)) *
+                        static_cast<float>(1 << o);
         n5 = o == 0 ? v : n5 + v;
     }
     Fe d5, d7;
@@ -150,15 +162,15 @@ __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz,
     float a1[N], a2[N], a3[N];
 #pragma unroll 1
     for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, axf(s.axis[ST_N2 + o][0][kx]), axf(s.axis[ST_N2 + o][1][kz]),
-                        s.yf[o], static_cast<float>(1 << o), a2, o == 0);
+        octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, ax_x(s, ST_N2 + o, kx), ax_z(s, ST_N2 + o, kz), s.yf[o],
+                        static_cast<float>(1 << o), a2, o == 0);
 #pragma unroll 1
     for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, axf(s.axis[ST_N3 + o][0][kx]), axf(s.axis[ST_N3 + o][1][kz]),
+        octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, ax_x(s, ST_N3 + o, kx), ax_z(s, ST_N3 + o, kz),
                         s.yf[16 + o], static_cast<float>(1 << o), a3, o == 0);
 #pragma unroll 1
     for (int o = 0; o < 8; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N1 + o) * PERM_BYTES, axf(s.axis[ST_N1 + o][0][kx]), axf(s.axis[ST_N1 + o][1][kz]),
+        octave3f<Y0, N>(s.perm + (ST_N1 + o) * PERM_BYTES, ax_x(s, ST_N1 + o, kx), ax_z(s, ST_N1 + o, kz),
                         s.yf[32 + o], static_cast<float>(1 << o), a1, o == 0);
     const Fe d5{shape[0], shape[1]}, d7{shape[2], shape[3]};
     unsigned b = 0;
@@ -172,15 +184,22 @@ __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz,
     return true;
 }
 
-__global__ void __launch_bounds__(CT, 1) k_coarse_signs_fast(StateCache cache, const RegionRef* __restrict__ queue,
+// CT threads per CTA (and columns per tile), MINB CTAs per SM: chosen by the autotuner.
+template <int CT, int MINB>
+__global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache, const RegionRef* __restrict__ queue,
                                                              const int* count, int maxCount,
-                                                             std::uint32_t* __restrict__ signs) {
+                                                             std::uint32_t* __restrict__ signs,
+                                                             unsigned long long* stats) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CoarseSmem& s = *reinterpret_cast<CoarseSmem*>(smem_raw);
     const int tid = threadIdx.x;
     const int jobs = min(*count, maxCount);
-    for (int job = blockIdx.x; job < jobs; job += gridDim.x) {
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
+    for (int item = blockIdx.x; item < jobs * 2; item += gridDim.x) {
+        const int job = item >> 1, half = item & 1;
         const RegionRef ref = queue[job];
+        const int row0 = half == 0 ? 0 : HALF_ROWS;
+        const int rows = half == 0 ? HALF_ROWS : SIDE - HALF_ROWS;
         const int originX = -28 + center_chunk_x(ref.center) * 4;
         const int originZ = -28 + center_chunk_z(ref.center) * 4;
         __syncthreads();
@@ -199,28 +218,43 @@ __global__ void __launch_bounds__(CT, 1) k_coarse_signs_fast(StateCache cache, c
             const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
             const double amp = 1.0 / static_cast<double>(1 << k);
             const double sy = o < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
-            build_yaxis(sy, s.off[o][1], s.y64[o]);
-            build_yf(s.y64[o], s.yf[o]);
+            YEntry ya[17];
+            build_yaxis(sy, s.off[o][1], ya);
+            build_yf(ya, s.yf[o]);
+            for (int y = 0; y < 17; ++y) s.y64[o][y] = Y64{ya[y].cellFrac, ya[y].fade};
         }
-        for (int e = tid; e < NOCT * 2 * SIDE; e += CT) {
-            const int o = e / (2 * SIDE), a = (e / SIDE) & 1, k = e % SIDE;
-            const double coord = static_cast<double>((a == 0 ? originX : originZ) + k);
-            const AxisF ax = make_axis(coord * octave_scale(o), s.off[o][a == 0 ? 0 : 2]);
-            s.axis[o][a][k] = AxisS{ax.f, ax.fd, ax.i};
+        for (int e = tid; e < NOCT * (rows + SIDE); e += CT) {
+            const int o = e / (rows + SIDE), k = e % (rows + SIDE);
+            if (k < rows) {
+                const AxisF ax = make_axis(static_cast<double>(originX + row0 + k) * octave_scale(o), s.off[o][0]);
+                s.xf[o][k] = ax.f;
+                s.xd[o][k] = ax.fd;
+                s.xi[o][k] = static_cast<std::uint8_t>(ax.i);
+            } else {
+                const int kz = k - rows;
+                const AxisF az = make_axis(static_cast<double>(originZ + kz) * octave_scale(o), s.off[o][2]);
+                s.zf[o][kz] = az.f;
+                s.zd[o][kz] = az.fd;
+                s.zi[o][kz] = static_cast<std::uint8_t>(az.i);
+            }
         }
         __syncthreads();
-        for (int base = 0; base < COLS; base += TILE) {
-            // column shapes (climate + noise4/5) of the tile
-            const int g = base + tid;
+        const int cols = rows * SIDE;
+        constexpr int TILE = CT;
+        for (int base = 0; base < cols; base += TILE) {
+            const int g = base + tid;  // half-local column: row g / SIDE, z g % SIDE
             s.mask[tid] = 0;
-            if (g < COLS) coarse_shape(s, originX, originZ, g / SIDE, g % SIDE, s.shape[tid]);
+            if (g < cols) {
+                const int kx = g / SIDE, kz = g % SIDE;
+                coarse_shape(s, originX + row0 + kx, originZ + kz, kx, kz, s.shape[tid]);
+            }
             __syncthreads();
-            // three Y ranges per column
             for (int t = tid; t < TILE * 3; t += CT) {
                 const int c = t % TILE, r = t / TILE;
                 const int gg = base + c;
-                if (gg >= COLS) continue;
+                if (gg >= cols) continue;
                 const int kx = gg / SIDE, kz = gg % SIDE;
+                atomicAdd(&s.screened, 1);
                 unsigned bits = 0;
                 bool ok;
                 if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
@@ -229,24 +263,31 @@ __global__ void __launch_bounds__(CT, 1) k_coarse_signs_fast(StateCache cache, c
                 if (ok) {
                     if (bits) atomicOr(&s.mask[c], bits);
                 } else {
+                    atomicAdd(&s.fallbacks, 1);
                     const int slot = atomicAdd(&s.fbCount, 1);
-                    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 16) | c);
-                    else atomicOr(&s.mask[c], exact_column(s, originX + kx, originZ + kz, r));
+                    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint16_t>((r << 12) | c);
+                    else atomicOr(&s.mask[c], exact_column(s, originX + row0 + kx, originZ + kz, r));
                 }
             }
             __syncthreads();
             const int nfb = min(s.fbCount, FB_CAP);
             for (int k = tid; k < nfb; k += CT) {
-                const std::uint32_t e = s.fb[k];
-                const int c = e & 0xFFFF, r = e >> 16;
+                const int e = s.fb[k];
+                const int c = e & 0xFFF, r = e >> 12;
                 const int gg = base + c;
-                atomicOr(&s.mask[c], exact_column(s, originX + gg / SIDE, originZ + gg % SIDE, r));
+                atomicOr(&s.mask[c], exact_column(s, originX + row0 + gg / SIDE, originZ + gg % SIDE, r));
             }
             __syncthreads();
-            if (g < COLS) signs[static_cast<std::size_t>(job) * COLS + g] = s.mask[tid];
+            if (g < cols)
+                signs[static_cast<std::size_t>(job) * COLS + static_cast<std::size_t>(row0) * SIDE + g] = s.mask[tid];
             if (tid == 0) s.fbCount = 0;
             __syncthreads();
         }
+    }
+    __syncthreads();
+    if (tid == 0 && stats) {
+        atomicAdd(&stats[2], static_cast<unsigned long long>(s.screened));
+        atomicAdd(&stats[3], static_cast<unsigned long long>(s.fallbacks));
     }
 }
 
@@ -258,23 +299,48 @@ void check(cudaError_t e, const char* what) {
     }
 }
 
-int g_sms = 0;
+struct Variant {
+    const char* name;
+    int threads;
+    void (*kernel)(StateCache, const RegionRef*, const int*, int, std::uint32_t*, unsigned long long*);
+    int grid;
+};
+Variant g_variants[] = {
+    {"512x1", 512, k_coarse_signs_fast<512, 1>, 0},
+    {"256x2", 256, k_coarse_signs_fast<256, 2>, 0},
+    {"384x1", 384, k_coarse_signs_fast<384, 1>, 0},
+    {"256x1", 256, k_coarse_signs_fast<256, 1>, 0},
+};
+constexpr int kVariants = sizeof(g_variants) / sizeof(g_variants[0]);
+int g_variant = 0;
 
 }  // namespace
 
+int coarse_fast_variants() { return kVariants; }
+const char* coarse_fast_variant_name(int v) { return g_variants[v].name; }
+void set_coarse_fast_variant(int v) { g_variant = (v >= 0 && v < kVariants) ? v : 0; }
+int get_coarse_fast_variant() { return g_variant; }
+
 void init_coarse_fast() {
-    check(cudaFuncSetAttribute(k_coarse_signs_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(CoarseSmem)),
-          "coarse fast smem");
-    int dev = 0;
+    int dev = 0, sms = 0;
     check(cudaGetDevice(&dev), "device");
-    check(cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+    for (Variant& v : g_variants) {
+        check(cudaFuncSetAttribute(v.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(CoarseSmem)),
+              "coarse fast smem");
+        int perSm = 0;
+        check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, v.kernel, v.threads, sizeof(CoarseSmem)),
+              "occupancy");
+        v.grid = sms * (perSm > 0 ? perSm : 1);
+    }
 }
 
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
-                              std::uint32_t* dSigns, cudaStream_t stream) {
+                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream) {
     if (maxCount <= 0) return;
-    const int grid = maxCount < g_sms ? maxCount : g_sms;
-    k_coarse_signs_fast<<<grid, CT, sizeof(CoarseSmem), stream>>>(cache, dQueue, dCount, maxCount, dSigns);
+    const Variant& v = g_variants[g_variant];
+    const int grid = 2 * maxCount < v.grid ? 2 * maxCount : v.grid;
+    v.kernel<<<grid, v.threads, sizeof(CoarseSmem), stream>>>(cache, dQueue, dCount, maxCount, dSigns, stats);
     check(cudaGetLastError(), "k_coarse_signs_fast");
 }
 

@@ -107,12 +107,30 @@ void launch_coarse_cc(const RegionRef* dQueue, const int* dCount, int maxCount, 
                       int* dLabelScratch, int* dStatScratch, RegionInfo* dRegions, int centers, cudaStream_t stream);
 
 // Screened (FP32 + exact fallback) kernels: identical outputs, far fewer FP64 operations.
+struct Stage0FastScratch {
+    RegionRef* p19Queue = nullptr;   // regions that passed the P20/Upper/High gates
+    std::uint8_t* highest = nullptr; // [slot][256] highest re-entry level per column (0xFF none)
+    int* p19Count = nullptr;
+    int p19Capacity = 0;
+    unsigned long long* stats = nullptr;  // [0] stage0 column tasks, [1] their FP64 fallbacks,
+                                          // [2] coarse column tasks, [3] their FP64 fallbacks
+};
 void init_stage0_fast();
 void launch_stage0_fast(const StateCache& cache, int n, int centers, const Profile& prof, RegionInfo* dRegions,
-                        RegionRef* dCoarseQueue, int* dCoarseCount, int coarseCapacity, cudaStream_t stream);
+                        RegionRef* dCoarseQueue, int* dCoarseCount, int coarseCapacity, const Stage0FastScratch& fs,
+                        cudaStream_t stream);
+// Launch-shape variants (threads x CTAs per SM) of the screened kernels, set by the autotuner.
+int stage0_fast_variants();
+const char* stage0_fast_variant_name(int v);
+void set_stage0_fast_variant(int v);
+int get_stage0_fast_variant();
+int coarse_fast_variants();
+const char* coarse_fast_variant_name(int v);
+void set_coarse_fast_variant(int v);
+int get_coarse_fast_variant();
 void init_coarse_fast();
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
-                              std::uint32_t* dSigns, cudaStream_t stream);
+                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream);
 int coarse_score_ctas();  // label/stat scratch is per CTA of the persistent score grid
 
 // Exact scan of one region at one radius; result in *dIsland (device).

@@ -75,7 +75,8 @@ typedef struct bsf_mega_record {
 typedef struct bsf_stage_counts {
     uint64_t worlds, regions, p20_passed, upper_passed, high_passed, p19_passed,
              mega_rejected, coarse_evaluated, coarse_passed, islands, rng_fallbacks,
-             lower_columns; /* lattice columns evaluated by the Lower stage */
+             lower_columns, /* lattice columns evaluated by the Lower stage */
+             screened_tasks, fallback_tasks; /* FP32-screened column tasks and those recomputed in FP64 */
 } bsf_stage_counts;
 
 /* Lifecycle. bsf_open returns NULL only when allocation of the handle itself fails;
@@ -147,6 +148,19 @@ uint64_t bsf_kernel_launches(const void* h);
  * ms[1] Stage0 + P19, ms[2] coarse, ms[3] exact stage (host wall time, it
  * includes its round trips). */
 int bsf_last_stage_ms(const void* h, float* ms4);
+
+/* Autotuner: times every launch-shape variant (threads per CTA x CTAs per SM)
+ * of the screened Stage0 and coarse kernels on `worlds` calibration worlds
+ * (capacity permitting) with CUDA events and keeps the fastest for this
+ * process. report (optional) receives "kernel: variant=ms ... -> choice". */
+int bsf_autotune(void* h, uint32_t worlds, char* report, size_t report_len);
+/* Selects launch-shape variants explicitly (index order of the autotune report). */
+int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_variant);
+
+/* Measured scalar FP64 and FP32 issue rates of the current device (instrumentation
+ * for the roofline): independent add chains in every lane of every SM, timed
+ * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
+int bsf_measure_peaks(double* ops_per_s2);
 
 /* Allocation-free variant of bsf_chunk_bitmaps. It has no counterpart in the
  * reference: it exists for callers that cannot allocate GPU memory (a host

@@ -45,7 +45,60 @@ def test_mega_search_forms_agree():
         w.set_mode(bsf.MODE_PLAIN)
         c2, r2 = w.mega_search(seeds)
     d1, d2 = c1.as_dict(), c2.as_dict()
-    d1.pop("rng_fallbacks"), d2.pop("rng_fallbacks")
+    for k in ("rng_fallbacks", "screened_tasks", "fallback_tasks"):  # instrumentation, not results
+        d1.pop(k), d2.pop(k)
     assert d1 == d2
+    # the screening must decide the vast majority of columns without FP64
+    assert c1.screened_tasks > 0 and c1.fallback_tasks < 0.01 * c1.screened_tasks
     assert [(r.world_index, r.center_index, r.coarse, r.island.key()) for r in r1] == \
            [(r.world_index, r.center_index, r.coarse, r.island.key()) for r in r2]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_every_launch_variant_gives_identical_records(variant):
+    seeds = consecutive(2048, 300 + variant)
+    with bsf.Worker(capacity=2048, profile="general", research=True, centers=8, max_exact_radius=1) as w:
+        w.set_mode(bsf.MODE_PLAIN)
+        exact = w.stage0_filter(seeds)
+        w.set_mode(bsf.MODE_QUEUED)
+        w.set_launch_variants(variant, variant)
+        fast = w.stage0_filter(seeds)
+        w.set_launch_variants(0, 0)
+    assert np.array_equal(fast, exact)
+
+
+def test_autotune_reports_and_keeps_results_exact():
+    seeds = consecutive(2048, 404)
+    with bsf.Worker(capacity=2048, profile="mega", research=True, centers=8, max_exact_radius=1) as w:
+        report = w.autotune(1024)
+        assert "stage0:" in report and "coarse:" in report and "->" in report
+        fast = w.stage0_filter(seeds)
+        w.set_mode(bsf.MODE_PLAIN)
+        exact = w.stage0_filter(seeds)
+    assert np.array_equal(fast, exact)
+
+
+def test_batch_graph_replays_match_first_capture():
+    """The queued mega batch runs as a cached CUDA graph keyed by batch size and
+    seed source: replays, other sizes and device-resident seeds agree with the
+    plain (uncaptured) form."""
+    torch = pytest.importorskip("torch")
+    seeds = consecutive(4096, 515)
+    with bsf.Worker(capacity=4096, profile="mega", centers=8, max_exact_radius=24) as w:
+        runs = []
+        for n in (4096, 1000, 4096, 1000):
+            before = w.kernel_launches
+            c, r = w.mega_search(seeds[:n])
+            runs.append((c.as_dict(), [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in r]))
+            # one graph replay = six kernels, plus the exact stage's own launches
+            assert w.kernel_launches - before >= 6
+        dev = torch.from_numpy(seeds).cuda()
+        torch.cuda.synchronize()
+        cd, rd = w.mega_search_device(dev.data_ptr(), len(seeds))
+        w.set_mode(bsf.MODE_PLAIN)
+        cp, rp = w.mega_search(seeds)
+    assert runs[0] == runs[2] and runs[1] == runs[3]
+    strip = lambda d: {k: v for k, v in d.items() if k not in ("rng_fallbacks", "screened_tasks", "fallback_tasks")}
+    assert strip(runs[0][0]) == strip(cp.as_dict()) == strip(cd.as_dict())
+    key = lambda rs: [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rs]
+    assert runs[0][1] == key(rp) == key(rd)
