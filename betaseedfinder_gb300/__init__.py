@@ -69,11 +69,45 @@ class StageCounts(ctypes.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("profile", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
+                ("chunk_worlds", ctypes.c_uint32), ("max_lanes", ctypes.c_int32),
+                ("max_preview_radius", ctypes.c_int32)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("status", ctypes.c_int32), ("queue_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double), ("records", ctypes.c_uint32), ("counts", StageCounts),
+                ("island", Island), ("preview_columns", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64 * 2), ("completed", ctypes.c_uint64 * 2),
+                ("failed", ctypes.c_uint64 * 2), ("p50_ms", ctypes.c_double * 2), ("p99_ms", ctypes.c_double * 2),
+                ("p999_ms", ctypes.c_double * 2), ("worlds_completed", ctypes.c_uint64),
+                ("hbm_bytes_in_use", ctypes.c_uint64), ("hbm_bytes_peak", ctypes.c_uint64),
+                ("hbm_budget", ctypes.c_uint64), ("lanes_open", ctypes.c_uint32 * 2),
+                ("max_busy_lanes", ctypes.c_uint32), ("deferred", ctypes.c_uint64), ("evictions", ctypes.c_uint64)]
+
+    def as_dict(self):
+        d = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            d[n] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+REQ_RANGE, REQ_PREVIEW = 0, 1
+PENDING = 1
+
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
-           "bsf_autotune", "bsf_set_launch_variants"]
+           "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
+           "bsf_set_stream_priority", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
+           "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
+           "bsf_server_records", "bsf_server_preview_columns", "bsf_server_release", "bsf_server_get_stats"]
 
 _lib = None
 
@@ -116,6 +150,24 @@ def load(path=LIB_PATH):
     L.bsf_measure_peaks.argtypes = [P(ctypes.c_double)]
     L.bsf_autotune.argtypes = [vp, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]
     L.bsf_set_launch_variants.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
+    L.bsf_config_footprint.argtypes = [P(Config), u64p]
+    L.bsf_handle_footprint.argtypes = [vp]
+    L.bsf_handle_footprint.restype = ctypes.c_uint64
+    L.bsf_set_stream_priority.argtypes = [vp, ctypes.c_int32]
+    L.bsf_default_server_config.argtypes = [P(ServerConfig)]
+    L.bsf_server_open.argtypes = [P(ServerConfig)]
+    L.bsf_server_open.restype = vp
+    L.bsf_server_close.argtypes = [vp]
+    L.bsf_server_last_error.argtypes = [vp]
+    L.bsf_server_last_error.restype = ctypes.c_char_p
+    L.bsf_server_submit_range.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, P(MatchSettings), u64p]
+    L.bsf_server_submit_preview.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                            P(MatchSettings), u64p]
+    L.bsf_server_poll.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32, P(ServerResult)]
+    L.bsf_server_records.argtypes = [vp, ctypes.c_uint64, P(MegaRecord), ctypes.c_uint32, P(ctypes.c_uint32)]
+    L.bsf_server_preview_columns.argtypes = [vp, ctypes.c_uint64, i32p, i32p, ctypes.c_uint32]
+    L.bsf_server_release.argtypes = [vp, ctypes.c_uint64]
+    L.bsf_server_get_stats.argtypes = [vp, P(ServerStats)]
     _lib = L
     return L
 
@@ -126,6 +178,20 @@ def measure_peaks():
     if load().bsf_measure_peaks(ops) != 0:
         raise BsfError("bsf_measure_peaks failed")
     return ops[0], ops[1]
+
+
+def config_footprint(capacity=32768, profile=PROFILE_MEGA, research=False, centers=8, max_exact_radius=24):
+    """Device bytes a Worker with this configuration allocates (no GPU needed)."""
+    L = load()
+    cfg = Config()
+    L.bsf_default_config(ctypes.byref(cfg))
+    cfg.capacity = capacity
+    cfg.profile = PROFILES.get(profile, profile) if isinstance(profile, str) else profile
+    cfg.research, cfg.centers, cfg.max_exact_radius = int(research), centers, max_exact_radius
+    b = ctypes.c_uint64(0)
+    if L.bsf_config_footprint(ctypes.byref(cfg), ctypes.byref(b)) != 0:
+        raise BsfError("bsf_config_footprint: bad config")
+    return int(b.value)
 
 
 def default_match_settings(**overrides):
@@ -199,6 +265,14 @@ class Worker:
 
     def set_launch_variants(self, stage0_variant, coarse_variant):
         self._check(load().bsf_set_launch_variants(self._h, stage0_variant, coarse_variant))
+
+    @property
+    def footprint(self):
+        """Device bytes this handle holds."""
+        return int(load().bsf_handle_footprint(self._h))
+
+    def set_stream_priority(self, high=True):
+        self._check(load().bsf_set_stream_priority(self._h, int(bool(high))))
 
     def last_stage_ms(self):
         """Per-stage device times of the last batch: setup, Stage0+P19, coarse, exact (ms)."""
@@ -277,6 +351,99 @@ class Worker:
                                                   ctypes.byref(s), recs, records_cap, ctypes.byref(n),
                                                   ctypes.byref(counts), ctypes.c_void_p(stream or 0)))
         return counts, [recs[i] for i in range(n.value)]
+
+
+class Server:
+    """Served mode (bsf_server_*): continuous batching of range searches and
+    previews over device-resident lanes, admitted by HBM footprint."""
+
+    def __init__(self, profile=PROFILE_MEGA, hbm_budget_bytes=0, chunk_worlds=8192, max_lanes=4,
+                 max_preview_radius=16, device=0):
+        L = load()
+        cfg = ServerConfig()
+        L.bsf_default_server_config(ctypes.byref(cfg))
+        cfg.device = device
+        cfg.profile = PROFILES.get(profile, profile) if isinstance(profile, str) else profile
+        cfg.hbm_budget_bytes, cfg.chunk_worlds, cfg.max_lanes = hbm_budget_bytes, chunk_worlds, max_lanes
+        cfg.max_preview_radius = max_preview_radius
+        self._s = L.bsf_server_open(ctypes.byref(cfg))
+        if not self._s:
+            raise BsfError("bsf_server_open failed")
+        err = L.bsf_server_last_error(self._s)
+        if err:
+            L.bsf_server_close(self._s)
+            self._s = None
+            raise BsfError("bsf_server_open: " + err.decode())
+
+    def close(self):
+        if self._s:
+            load().bsf_server_close(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, status):
+        if status < 0:
+            raise BsfError("status %d: %s" % (status, load().bsf_server_last_error(self._s).decode()))
+        return status
+
+    def last_error(self):
+        return load().bsf_server_last_error(self._s).decode()
+
+    def submit_range(self, seeds, radius=7, settings=None):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        t = ctypes.c_uint64(0)
+        s = settings or default_match_settings()
+        self._check(load().bsf_server_submit_range(self._s, _p(seeds, ctypes.c_int64), len(seeds), radius,
+                                                   ctypes.byref(s), ctypes.byref(t)))
+        return int(t.value)
+
+    def submit_preview(self, seed, center_chunk_x=0, center_chunk_z=0, radius=7, settings=None):
+        t = ctypes.c_uint64(0)
+        s = settings or default_match_settings()
+        self._check(load().bsf_server_submit_preview(self._s, seed, center_chunk_x, center_chunk_z, radius,
+                                                     ctypes.byref(s), ctypes.byref(t)))
+        return int(t.value)
+
+    def poll(self, ticket, wait_ms=0):
+        """ServerResult when finished, None while pending."""
+        r = ServerResult()
+        st = self._check(load().bsf_server_poll(self._s, ticket, wait_ms, ctypes.byref(r)))
+        return None if st == PENDING else r
+
+    def wait(self, ticket):
+        return self.poll(ticket, -1)
+
+    def records(self, ticket, cap=1 << 16):
+        recs = (MegaRecord * cap)()
+        n = ctypes.c_uint32(0)
+        self._check(load().bsf_server_records(self._s, ticket, recs, cap, ctypes.byref(n)))
+        return [recs[i] for i in range(n.value)]
+
+    def preview_columns(self, ticket, cells):
+        mn = np.zeros(max(cells, 1), np.int32)
+        mx = np.zeros(max(cells, 1), np.int32)
+        self._check(load().bsf_server_preview_columns(self._s, ticket, _p(mn, ctypes.c_int32),
+                                                      _p(mx, ctypes.c_int32), max(cells, 1)))
+        return mn[:cells], mx[:cells]
+
+    def release(self, ticket):
+        self._check(load().bsf_server_release(self._s, ticket))
+
+    def stats(self):
+        st = ServerStats()
+        self._check(load().bsf_server_get_stats(self._s, ctypes.byref(st)))
+        return st
 
 
 class GpuStage0Scout:

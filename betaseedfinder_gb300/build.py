@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
 CU_SOURCES = ["bsf_stage0.cu", "bsf_stage0_fast.cu", "bsf_coarse.cu", "bsf_coarse_fast.cu", "bsf_exact.cu",
-              "bsf_api.cu", "bsf_noalloc.cu"]
+              "bsf_api.cu", "bsf_noalloc.cu", "bsf_server.cu"]
 LIB = os.path.join(BUILD, "libbsf.so")
 WORKER = os.path.join(BUILD, "bsf_worker")
 
@@ -69,7 +69,7 @@ def build(verbose=False, extra_flags=()):
     if _stale(LIB, objs):
         tmp = LIB + ".tmp"
         subprocess.check_call([cc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", tmp, *objs,
-                               "-lcudart"])
+                               "-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
     wsrc = os.path.join(CSRC, "bsf_worker.cpp")
     if _stale(WORKER, [wsrc, LIB, os.path.join(ROOT, "include", "bsf.h")]):

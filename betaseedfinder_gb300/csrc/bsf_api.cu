@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <shared_mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -121,6 +123,17 @@ __global__ void k_add_chains(T* out, int iters, T inc) {
 
 using namespace bsf;
 
+// Stream capture versus device-wide calls. While any thread captures a stream,
+// calls that synchronise the device (cudaFree, cudaDeviceSynchronize) fail and
+// break the capture, so handles open and close under the exclusive side of this
+// lock and batch graphs are captured under the shared side: handles on several
+// threads (the served mode's lanes) can capture at once but never while another
+// thread allocates or frees a handle.
+static std::shared_mutex& capture_guard() {
+    static std::shared_mutex m;
+    return m;
+}
+
 struct BsfHandle {
     bsf_config cfg{};
     Profile prof{};
@@ -142,6 +155,7 @@ struct BsfHandle {
     std::uint32_t* dSigns = nullptr;
     int* dLabels = nullptr;
     int* dStats = nullptr;
+    int* dCoarseErr = nullptr;  // coarse union-find retry-bound flag (inside dStats)
     std::uint8_t* dOut = nullptr;
     std::uint64_t* dHashes = nullptr;
     unsigned long long* dStageCounts = nullptr;
@@ -159,7 +173,8 @@ struct BsfHandle {
     std::vector<RegionInfo> hRegions;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stageMs[4] = {0, 0, 0, 0};
-    unsigned long long* hPinned = nullptr;  // stage counters [0..7], screen stats [8..11], counters [12..13]
+    unsigned long long* hPinned = nullptr;  // stage counters [0..7], screen stats [8..11], counters [12..13],
+                                            // coarse retry flag [14]
     struct CachedGraph {
         cudaGraphExec_t exec;
         cudaStream_t stream;
@@ -172,7 +187,14 @@ struct BsfHandle {
         graphs.clear();
     }
 
-    void alloc(void** p, std::size_t bytes, const char* what) { check(cudaMalloc(p, bytes), what); }
+    std::size_t footprint = 0;  // device bytes allocated by the handle
+    bool dry = false;           // size the buffers without allocating them
+
+    void alloc(void** p, std::size_t bytes, const char* what) {
+        if (dry) *p = nullptr;
+        else check(cudaMalloc(p, bytes), what);
+        footprint += bytes;
+    }
 };
 
 namespace {
@@ -319,6 +341,13 @@ void run_gpu_stages_timed(BsfHandle* h, int n) {
     run_gpu_stages_queued(h, n, true);
 }
 
+// Blocking device-to-host read on the handle's own stream (never the legacy
+// default stream, which handles on other threads must not wait on).
+void d2h(BsfHandle* h, void* dst, const void* src, std::size_t bytes, const char* what) {
+    check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream), what);
+    check(cudaStreamSynchronize(h->stream), what);
+}
+
 void read_stage_times(BsfHandle* h) {
     for (int i = 0; i < 2; ++i) check(cudaEventElapsedTime(&h->stageMs[i], h->ev[i], h->ev[i + 1]), "event time");
     check(cudaEventElapsedTime(&h->stageMs[2], h->ev[2], h->ev[3]), "event time");
@@ -333,7 +362,7 @@ Island exact_once(BsfHandle* h, int world, int ccx, int ccz, int radius, const M
     check(cudaMemcpyAsync(&isl, h->dIsland, sizeof(Island), cudaMemcpyDeviceToHost, h->stream), "island download");
     check(cudaStreamSynchronize(h->stream), "exact scan");
     int err = 0;
-    check(cudaMemcpy(&err, h->exact.err, sizeof(int), cudaMemcpyDeviceToHost), "err");
+    d2h(h, &err, h->exact.err, sizeof(int), "err");
     if (err) throw std::runtime_error("exact scan union-find exceeded its retry bound");
     return isl;
 }
@@ -392,6 +421,7 @@ void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seed
     check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
     check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
     check(cudaMemsetAsync(h->fs.stats, 0, 4 * sizeof(unsigned long long), h->stream), "memset");
+    check(cudaMemsetAsync(h->dCoarseErr, 0, sizeof(int), h->stream), "memset");
     record(h, 0);
     if (seedSource == 2) {
         check(cudaMemcpyAsync(h->dSeeds, h->hSeeds, static_cast<std::size_t>(n) * 8, cudaMemcpyHostToDevice,
@@ -416,6 +446,8 @@ void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seed
     check(cudaMemcpyAsync(h->hPinned + 8, h->fs.stats, 4 * 8, cudaMemcpyDeviceToHost, h->stream), "screen stats");
     check(cudaMemcpyAsync(h->hPinned + 12, h->dCounters, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->stream),
           "counts");
+    check(cudaMemcpyAsync(h->hPinned + 14, h->dCoarseErr, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+          "coarse flag");
 }
 
 // Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters.
@@ -428,6 +460,7 @@ cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
     const unsigned long long launchesBefore = h->launches;
     cudaGraph_t graph = nullptr;
+    std::shared_lock<std::shared_mutex> captureLock(capture_guard());
     check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
     try {
         enqueue_batch(h, n, hostSeeds ? 2 : 0, nullptr);
@@ -477,20 +510,24 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     const int* hcount = reinterpret_cast<const int*>(h->hPinned + 12);
     check(cudaStreamSynchronize(h->stream), "mega batch");
     if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
+    if (*reinterpret_cast<const int*>(h->hPinned + 14))
+        throw std::runtime_error("coarse union-find exceeded its retry bound");
     read_stage_times(h);
     const auto exactStart = std::chrono::steady_clock::now();
     const int exactN = std::min(hcount[2], h->exactCap);
     std::vector<RegionRef> ex(exactN);
     std::vector<RegionInfo> info(exactN);
     if (exactN) {
-        check(cudaMemcpy(ex.data(), h->dExactQueue, sizeof(RegionRef) * exactN, cudaMemcpyDeviceToHost), "exact list");
+        d2h(h, ex.data(), h->dExactQueue, sizeof(RegionRef) * exactN, "exact list");
         std::sort(ex.begin(), ex.end(), [](const RegionRef& a, const RegionRef& b) {
             return a.world != b.world ? a.world < b.world : a.center < b.center;
         });
         for (int k = 0; k < exactN; ++k)
-            check(cudaMemcpy(&info[k], h->dRegions + static_cast<std::size_t>(ex[k].world) * h->centers + ex[k].center,
-                             sizeof(RegionInfo), cudaMemcpyDeviceToHost),
+            check(cudaMemcpyAsync(&info[k],
+                                  h->dRegions + static_cast<std::size_t>(ex[k].world) * h->centers + ex[k].center,
+                                  sizeof(RegionInfo), cudaMemcpyDeviceToHost, h->stream),
                   "region info");
+        check(cudaStreamSynchronize(h->stream), "region info");
     }
     unsigned long long islands = 0;
     uint32_t written = 0;
@@ -502,7 +539,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
             bsf_mega_record& r = records[written++];
             std::int64_t seed = 0;
             if (hostSeeds) seed = seeds[ex[k].world];
-            else check(cudaMemcpy(&seed, seeds + ex[k].world, 8, cudaMemcpyDeviceToHost), "seed");
+            else d2h(h, &seed, seeds + ex[k].world, 8, "seed");
             r.seed = seed;
             r.world_index = ex[k].world;
             r.center_index = ex[k].center;
@@ -538,6 +575,73 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     return BSF_OK;
 }
 
+// Every device buffer of a handle, sized from its config. With h->dry set this
+// only sums the sizes (bsf_config_footprint); otherwise it allocates them.
+void open_buffers(BsfHandle* h, const bsf_config& cfg) {
+    h->capacity = static_cast<int>(cfg.capacity);
+    h->centers = cfg.centers;
+    h->prof = profile_by_id(cfg.profile);
+    const std::size_t n = static_cast<std::size_t>(h->capacity);
+    const std::size_t regions = n * h->centers;
+    h->coarseCap = static_cast<int>(std::min<std::size_t>(regions, 1u << 14));
+    h->exactCap = 4096;
+    h->alloc(reinterpret_cast<void**>(&h->dSeeds), n * 8, "seeds");
+    h->alloc(reinterpret_cast<void**>(&h->cache.perms), n * WORLD_PERM_BYTES, "state cache");
+    h->alloc(reinterpret_cast<void**>(&h->cache.offsets), n * WORLD_OFFSETS * 8, "state cache");
+    h->cache.capacity = h->capacity;
+    h->alloc(reinterpret_cast<void**>(&h->dRegions), regions * sizeof(RegionInfo), "regions");
+    h->alloc(reinterpret_cast<void**>(&h->dCoarseQueue), regions * sizeof(RegionRef), "coarse queue");
+    h->alloc(reinterpret_cast<void**>(&h->dCounters), 16 * sizeof(int), "counters");
+    const std::size_t cc = static_cast<std::size_t>(h->coarseCap);
+    h->alloc(reinterpret_cast<void**>(&h->dSigns), cc * 61 * 61 * 4, "coarse signs");
+    const std::size_t ctas = static_cast<std::size_t>(coarse_score_ctas(h->coarseCap));
+    h->alloc(reinterpret_cast<void**>(&h->dLabels), ctas * 61 * 61 * 17 * 4, "coarse labels");
+    h->alloc(reinterpret_cast<void**>(&h->dStats), ctas * 61 * 61 * 17 * 8 + 64, "coarse stats");
+    if (!h->dry) h->dCoarseErr = h->dStats + ctas * 61 * 61 * 17 * 2;
+    h->outBytes = regions * (cfg.research ? 34 : 16) + 64;
+    h->alloc(reinterpret_cast<void**>(&h->dOut), std::max<std::size_t>(h->outBytes, n * 4096), "output");
+    h->alloc(reinterpret_cast<void**>(&h->dHashes), n * 8, "hashes");
+    h->alloc(reinterpret_cast<void**>(&h->dStageCounts), 8 * sizeof(unsigned long long), "stage counts");
+    h->alloc(reinterpret_cast<void**>(&h->dExactQueue), h->exactCap * sizeof(RegionRef), "exact queue");
+    h->fs.p19Capacity = static_cast<int>(regions);
+    h->alloc(reinterpret_cast<void**>(&h->fs.p19Queue), regions * sizeof(RegionRef), "p19 queue");
+    h->alloc(reinterpret_cast<void**>(&h->fs.highest), regions * 256, "p19 grids");
+    h->alloc(reinterpret_cast<void**>(&h->fs.p19Count), 64, "p19 count");
+    h->alloc(reinterpret_cast<void**>(&h->fs.stats), 8 * sizeof(unsigned long long), "screen stats");
+    if (!h->dry) check(cudaMemsetAsync(h->fs.stats, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
+    const std::size_t eb = exact_scratch_bytes(cfg.max_exact_radius);
+    h->alloc(&h->dExactBase, eb, "exact scratch");
+    if (!h->dry) {
+        exact_scratch_carve(h->exact, h->dExactBase, cfg.max_exact_radius);
+        check(cudaMemsetAsync(h->exact.err, 0, 64, h->stream), "memset");
+    }
+    h->alloc(reinterpret_cast<void**>(&h->dIsland), sizeof(Island), "island");
+    h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
+    h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+    h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+}
+
+// Constant tables and kernel attributes, once per device: handles opened later
+// (from any thread) must not rewrite constant memory under running kernels.
+void init_device_once(int device) {
+    static std::mutex mu;
+    static std::vector<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), device) != done.end()) return;
+    init_lcg_tables();
+    init_stage0_fast();
+    init_coarse_fast();
+    done.push_back(device);
+}
+
+void validate_config(const bsf_config& cfg) {
+    if (cfg.capacity < 1 || cfg.capacity > (1u << 22)) throw std::invalid_argument("capacity must be 1..4194304");
+    if (cfg.centers != 1 && cfg.centers != 8) throw std::invalid_argument("centers must be 1 or 8");
+    if (cfg.profile < 0 || cfg.profile > 3) throw std::invalid_argument("profile must be 0..3");
+    if (cfg.max_exact_radius < 1 || cfg.max_exact_radius > 24)
+        throw std::invalid_argument("max_exact_radius must be 1..24");
+}
+
 }  // namespace
 
 extern "C" {
@@ -569,61 +673,20 @@ void* bsf_open(const bsf_config* cfgIn) {
     bsf_default_config(&cfg);
     if (cfgIn) cfg = *cfgIn;
     h->cfg = cfg;
+    std::unique_lock<std::shared_mutex> allocLock(capture_guard());
     try {
-        if (cfg.capacity < 1 || cfg.capacity > (1u << 22)) throw std::invalid_argument("capacity must be 1..4194304");
-        if (cfg.centers != 1 && cfg.centers != 8) throw std::invalid_argument("centers must be 1 or 8");
-        if (cfg.profile < 0 || cfg.profile > 3) throw std::invalid_argument("profile must be 0..3");
-        if (cfg.max_exact_radius < 1 || cfg.max_exact_radius > 24)
-            throw std::invalid_argument("max_exact_radius must be 1..24");
+        validate_config(cfg);
         check(cudaSetDevice(cfg.device), "cudaSetDevice");
         check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
-        init_lcg_tables();
-        init_stage0_fast();
-        init_coarse_fast();
-        h->capacity = static_cast<int>(cfg.capacity);
-        h->centers = cfg.centers;
-        h->prof = profile_by_id(cfg.profile);
+        init_device_once(cfg.device);
+        open_buffers(h, cfg);
         const std::size_t n = static_cast<std::size_t>(h->capacity);
-        const std::size_t regions = n * h->centers;
-        h->coarseCap = static_cast<int>(std::min<std::size_t>(regions, 1u << 14));
-        h->exactCap = 4096;
-        h->alloc(reinterpret_cast<void**>(&h->dSeeds), n * 8, "seeds");
-        h->alloc(reinterpret_cast<void**>(&h->cache.perms), n * WORLD_PERM_BYTES, "state cache");
-        h->alloc(reinterpret_cast<void**>(&h->cache.offsets), n * WORLD_OFFSETS * 8, "state cache");
-        h->cache.capacity = h->capacity;
-        h->alloc(reinterpret_cast<void**>(&h->dRegions), regions * sizeof(RegionInfo), "regions");
-        h->alloc(reinterpret_cast<void**>(&h->dCoarseQueue), regions * sizeof(RegionRef), "coarse queue");
-        h->alloc(reinterpret_cast<void**>(&h->dCounters), 16 * sizeof(int), "counters");
-        const std::size_t cc = static_cast<std::size_t>(h->coarseCap);
-        h->alloc(reinterpret_cast<void**>(&h->dSigns), cc * 61 * 61 * 4, "coarse signs");
-        const std::size_t ctas = static_cast<std::size_t>(coarse_score_ctas());
-        h->alloc(reinterpret_cast<void**>(&h->dLabels), ctas * 61 * 61 * 17 * 4, "coarse labels");
-        h->alloc(reinterpret_cast<void**>(&h->dStats), ctas * 61 * 61 * 17 * 8 + 64, "coarse stats");
-        h->outBytes = regions * (cfg.research ? 34 : 16) + 64;
-        h->alloc(reinterpret_cast<void**>(&h->dOut), std::max<std::size_t>(h->outBytes, n * 4096), "output");
-        h->alloc(reinterpret_cast<void**>(&h->dHashes), n * 8, "hashes");
-        h->alloc(reinterpret_cast<void**>(&h->dStageCounts), 8 * sizeof(unsigned long long), "stage counts");
-        h->alloc(reinterpret_cast<void**>(&h->dExactQueue), h->exactCap * sizeof(RegionRef), "exact queue");
-        h->fs.p19Capacity = static_cast<int>(regions);
-        h->alloc(reinterpret_cast<void**>(&h->fs.p19Queue), regions * sizeof(RegionRef), "p19 queue");
-        h->alloc(reinterpret_cast<void**>(&h->fs.highest), regions * 256, "p19 grids");
-        h->alloc(reinterpret_cast<void**>(&h->fs.p19Count), 64, "p19 count");
-        h->alloc(reinterpret_cast<void**>(&h->fs.stats), 8 * sizeof(unsigned long long), "screen stats");
-        check(cudaMemset(h->fs.stats, 0, 8 * sizeof(unsigned long long)), "memset");
-        const std::size_t eb = exact_scratch_bytes(cfg.max_exact_radius);
-        h->alloc(&h->dExactBase, eb, "exact scratch");
-        exact_scratch_carve(h->exact, h->dExactBase, cfg.max_exact_radius);
-        check(cudaMemset(h->exact.err, 0, 64), "memset");
-        h->alloc(reinterpret_cast<void**>(&h->dIsland), sizeof(Island), "island");
-        h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
-        h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
-        h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
         for (auto& e : h->ev) check(cudaEventCreate(&e), "event");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hSeeds), n * 8), "pinned seeds");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hPinned), 16 * sizeof(unsigned long long)), "pinned counters");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
               "pinned output");
-        check(cudaDeviceSynchronize(), "open");
+        check(cudaStreamSynchronize(h->stream), "open");
         h->ok = true;
     } catch (const std::exception& e) {
         h->err = e.what();
@@ -636,6 +699,7 @@ void bsf_close(void* hv) {
     BsfHandle* h = static_cast<BsfHandle*>(hv);
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    std::unique_lock<std::shared_mutex> allocLock(capture_guard());
     h->drop_graphs();
     void* dev[] = {h->dSeeds, h->cache.perms, h->cache.offsets, h->dRegions, h->dCoarseQueue, h->dCounters,
                    h->dSigns, h->dLabels, h->dStats, h->dOut, h->dHashes, h->dStageCounts, h->dExactQueue,
@@ -650,6 +714,40 @@ void bsf_close(void* hv) {
     if (h->hPinned) cudaFreeHost(h->hPinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+}
+
+int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
+    if (!cfg || !bytes) return BSF_E_ARG;
+    try {
+        validate_config(*cfg);
+        BsfHandle h;
+        h.dry = true;
+        open_buffers(&h, *cfg);
+        *bytes = h.footprint;
+        return BSF_OK;
+    } catch (const std::exception&) {
+        return BSF_E_ARG;
+    }
+}
+
+uint64_t bsf_handle_footprint(const void* hv) {
+    const BsfHandle* h = static_cast<const BsfHandle*>(hv);
+    return h ? h->footprint : 0;
+}
+
+int bsf_set_stream_priority(void* hv, int32_t high) {
+    return guarded(hv, [&](BsfHandle* h) {
+        int least = 0, greatest = 0;
+        check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "priority range");
+        cudaStream_t s = nullptr;
+        std::unique_lock<std::shared_mutex> allocLock(capture_guard());
+        check(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, high ? greatest : least), "stream");
+        check(cudaStreamSynchronize(h->stream), "stream");
+        h->drop_graphs();
+        cudaStreamDestroy(h->stream);
+        h->stream = s;
+        return BSF_OK;
+    });
 }
 
 const char* bsf_last_error(const void* hv) {
@@ -730,7 +828,7 @@ int bsf_chunk_bitmaps(void* hv, const int64_t* seeds, uint32_t count, int32_t ch
               "bitmap download");
         check(cudaStreamSynchronize(h->stream), "chunk bitmaps");
         std::memcpy(bitmaps, h->hOut, static_cast<std::size_t>(n) * 4096);
-        if (hashes) check(cudaMemcpy(hashes, h->dHashes, static_cast<std::size_t>(n) * 8, cudaMemcpyDeviceToHost), "hashes");
+        if (hashes) d2h(h, hashes, h->dHashes, static_cast<std::size_t>(n) * 8, "hashes");
         return BSF_OK;
     });
 }
@@ -771,8 +869,8 @@ int bsf_preview(void* hv, int64_t seed, int32_t ccx, int32_t ccz, int32_t radius
         if (!isl.found) return BSF_OK;
         const std::size_t cells = static_cast<std::size_t>(isl.maxX - isl.minX + 1) * (isl.maxZ - isl.minZ + 1);
         if (cells > capacity) throw std::length_error("bsf_preview: capacity smaller than the island footprint");
-        check(cudaMemcpy(minY, h->dPrevMin, cells * 4, cudaMemcpyDeviceToHost), "preview");
-        check(cudaMemcpy(maxY, h->dPrevMax, cells * 4, cudaMemcpyDeviceToHost), "preview");
+        d2h(h, minY, h->dPrevMin, cells * 4, "preview");
+        d2h(h, maxY, h->dPrevMax, cells * 4, "preview");
         return BSF_OK;
     });
 }

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <stdexcept>
 
 namespace bsf {
@@ -335,14 +336,14 @@ void check(cudaError_t e, const char* what) {
     }
 }
 
-bool g_attrs = false;
+std::once_flag g_attrs;  // handles on several threads launch these kernels
 void ensure_attrs() {
-    if (g_attrs) return;
-    check(cudaFuncSetAttribute(k_coarse_signs, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(LatticeSmem)),
-          "coarse smem");
-    check(cudaFuncSetAttribute(k_lattice_noise, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(LatticeSmem)),
-          "lattice smem");
-    g_attrs = true;
+    std::call_once(g_attrs, [] {
+        check(cudaFuncSetAttribute(k_coarse_signs, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(LatticeSmem)),
+              "coarse smem");
+        check(cudaFuncSetAttribute(k_lattice_noise, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(LatticeSmem)),
+              "lattice smem");
+    });
 }
 
 }  // namespace
@@ -351,7 +352,7 @@ std::size_t coarse_scratch_bytes_per_region() {
     return static_cast<std::size_t>(COARSE_COLS) * 4 + static_cast<std::size_t>(COARSE_CELLS) * 4 * 3;
 }
 
-int coarse_score_ctas() { return COARSE_SCORE_CTAS; }
+int coarse_score_ctas(int maxCount) { return std::min(maxCount, COARSE_SCORE_CTAS); }
 
 void launch_coarse_score(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
                          const LatticeBuffers&, std::uint32_t* dSignScratch, int* dLabelScratch, int* dStatScratch,
@@ -362,8 +363,9 @@ void launch_coarse_score(const StateCache& cache, const RegionRef* dQueue, const
     const int signGrid = std::min(maxCount * tilesPerJob, 152 * 4);
     k_coarse_signs<<<signGrid, 256, sizeof(LatticeSmem), stream>>>(cache, dQueue, dCount, maxCount, dSignScratch);
     check(cudaGetLastError(), "k_coarse_signs");
-    int* err = dStatScratch + static_cast<std::size_t>(COARSE_SCORE_CTAS) * COARSE_CELLS * 2;
-    k_coarse_score<<<std::min(maxCount, COARSE_SCORE_CTAS), CC_THREADS, 0, stream>>>(
+    // the retry-bound flag sits right after the per-CTA scratch of the grid
+    int* err = dStatScratch + static_cast<std::size_t>(coarse_score_ctas(maxCount)) * COARSE_CELLS * 2;
+    k_coarse_score<<<coarse_score_ctas(maxCount), CC_THREADS, 0, stream>>>(
         dSignScratch, dQueue, dCount, maxCount, dLabelScratch, dStatScratch, dRegions, centers, err);
     check(cudaGetLastError(), "k_coarse_score");
 }
@@ -371,8 +373,9 @@ void launch_coarse_score(const StateCache& cache, const RegionRef* dQueue, const
 void launch_coarse_cc(const RegionRef* dQueue, const int* dCount, int maxCount, std::uint32_t* dSignScratch,
                       int* dLabelScratch, int* dStatScratch, RegionInfo* dRegions, int centers, cudaStream_t stream) {
     if (maxCount <= 0) return;
-    int* err = dStatScratch + static_cast<std::size_t>(COARSE_SCORE_CTAS) * COARSE_CELLS * 2;
-    k_coarse_score<<<std::min(maxCount, COARSE_SCORE_CTAS), CC_THREADS, 0, stream>>>(
+    // the retry-bound flag sits right after the per-CTA scratch of the grid
+    int* err = dStatScratch + static_cast<std::size_t>(coarse_score_ctas(maxCount)) * COARSE_CELLS * 2;
+    k_coarse_score<<<coarse_score_ctas(maxCount), CC_THREADS, 0, stream>>>(
         dSignScratch, dQueue, dCount, maxCount, dLabelScratch, dStatScratch, dRegions, centers, err);
     check(cudaGetLastError(), "k_coarse_score");
 }

@@ -16,6 +16,7 @@
 
 #include <climits>
 #include <cstdio>
+#include <mutex>
 #include <stdexcept>
 
 namespace bsf {
@@ -480,12 +481,11 @@ void launch_exact_scan(const StateCache& cache, int world, int ccx, int ccz, int
         LatticeJob job{world, (ccx - radius) * 4, (ccz - radius) * 4, d.side};
         launch_lattice_noise_one(cache, job, lat, stream);
     }
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag attr;  // handles on several threads launch this kernel
+    std::call_once(attr, [] {
         check(cudaFuncSetAttribute(k_exact_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(ChunkSmem)),
               "exact smem");
-        attr = true;
-    }
+    });
     k_exact_chunks<<<d.nc * d.nc, 128, sizeof(ChunkSmem), stream>>>(cache, world, d, lat, s.stone);
     check(cudaGetLastError(), "k_exact_chunks");
     int* aux = s.compStats;

@@ -131,7 +131,10 @@ int get_coarse_fast_variant();
 void init_coarse_fast();
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
                               std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream);
-int coarse_score_ctas();  // label/stat scratch is per CTA of the persistent score grid
+// Persistent coarse-score grid for a queue of maxCount regions: label/stat scratch
+// is per CTA (COARSE_CELLS ints of labels, 2 * COARSE_CELLS of stats) and the
+// union-find retry-bound flag (one int) follows the stat scratch.
+int coarse_score_ctas(int maxCount);
 
 // Exact scan of one region at one radius; result in *dIsland (device).
 struct ExactScratch {

@@ -162,6 +162,85 @@ int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_vari
  * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
 int bsf_measure_peaks(double* ops_per_s2);
 
+/* Device memory (bytes) a handle opened with cfg allocates, computed without a
+ * GPU from the same buffer list bsf_open allocates; BSF_E_ARG for a bad config. */
+int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes);
+/* Device memory (bytes) this handle holds. */
+uint64_t bsf_handle_footprint(const void* h);
+/* Moves the handle's work to a new stream of the device's highest (high != 0) or
+ * default (high == 0) priority; the block scheduler starts pending CTAs of a
+ * higher-priority stream first. Must not be called while the handle is in use. */
+int bsf_set_stream_priority(void* h, int32_t high);
+
+/* ---- Served mode (bsf_server_*) ------------------------------------------
+ * A request loop that keeps generator caches, stage queues and scratch
+ * resident on the device in "lanes" (one handle + stream each) and runs two
+ * request classes concurrently:
+ *   RANGE   a MEGA search over a list of seeds (IslandSearchEngine's GPU range
+ *           scan, src/IslandSearchEngine.java:1252-1255 / 1878-1971), split
+ *           into chunks of chunk_worlds worlds;
+ *   PREVIEW one island preview (generate3DPreviewForIsland -> buildIsland3DData,
+ *           src/IslandSearchEngine.java:284-436).
+ * Continuous batching: a request is admitted as soon as a lane is idle, or a
+ * new lane's device footprint (bsf_config_footprint) fits in the HBM budget
+ * (idle lanes of the other class are closed to make room); range requests
+ * are handed out one chunk at a time, so requests that arrive later start
+ * while earlier ones are still on the GPU, previews first. Preview lanes run
+ * on high-priority streams. Results do not depend on what else is running:
+ * every lane computes with its own buffers. Records of a range request come
+ * back in (world_index, center_index) order like bsf_mega_search. */
+#define BSF_PENDING 1 /* bsf_server_poll: not finished within the wait */
+#define BSF_REQ_RANGE 0
+#define BSF_REQ_PREVIEW 1
+
+typedef struct bsf_server_config {
+    int32_t device;
+    int32_t profile;             /* BSF_PROFILE_* of range searches */
+    uint64_t hbm_budget_bytes;   /* device bytes all lanes may hold; 0 = half the free memory at open */
+    uint32_t chunk_worlds;       /* range lane capacity = worlds per chunk (default 8192) */
+    int32_t max_lanes;           /* lanes busy at once = worker threads (default 4) */
+    int32_t max_preview_radius;  /* largest preview radius (default 16, at most 24) */
+} bsf_server_config;
+
+typedef struct bsf_server_result {
+    int32_t kind;                /* BSF_REQ_* */
+    int32_t status;              /* BSF_OK or the failing call's BSF_E_* */
+    double queue_ms;             /* submit -> first work on a lane */
+    double latency_ms;           /* submit -> completion */
+    uint32_t records;            /* RANGE: records available from bsf_server_records */
+    bsf_stage_counts counts;     /* RANGE: summed over chunks */
+    bsf_island island;           /* PREVIEW: the chosen island */
+    uint32_t preview_columns;    /* PREVIEW: width * depth entries of bsf_server_preview_columns */
+} bsf_server_result;
+
+typedef struct bsf_server_stats {
+    uint64_t submitted[2], completed[2], failed[2]; /* by BSF_REQ_* */
+    double p50_ms[2], p99_ms[2], p999_ms[2];        /* latency of completed requests */
+    uint64_t worlds_completed;                       /* RANGE worlds finished */
+    uint64_t hbm_bytes_in_use, hbm_bytes_peak, hbm_budget;
+    uint32_t lanes_open[2];
+    uint32_t max_busy_lanes;                         /* most lanes running work at one time */
+    uint64_t deferred;                               /* admissions that waited for memory or a lane */
+    uint64_t evictions;                              /* idle lanes closed to admit the other class */
+} bsf_server_stats;
+
+void bsf_default_server_config(bsf_server_config* cfg);
+void* bsf_server_open(const bsf_server_config* cfg);
+void bsf_server_close(void* s); /* waits for running work; pending requests are dropped */
+const char* bsf_server_last_error(const void* s);
+/* Submit calls copy their inputs and return at once with a ticket. */
+int bsf_server_submit_range(void* s, const int64_t* seeds, uint32_t count, int32_t radius,
+                            const bsf_match_settings* ms, uint64_t* ticket);
+int bsf_server_submit_preview(void* s, int64_t seed, int32_t center_chunk_x, int32_t center_chunk_z,
+                              int32_t radius, const bsf_match_settings* ms, uint64_t* ticket);
+/* Waits up to wait_ms (0 = no wait, < 0 = forever) for the ticket: BSF_OK with
+ * out filled when finished, BSF_PENDING when not yet, BSF_E_ARG for an unknown ticket. */
+int bsf_server_poll(void* s, uint64_t ticket, int32_t wait_ms, bsf_server_result* out);
+int bsf_server_records(void* s, uint64_t ticket, bsf_mega_record* out, uint32_t cap, uint32_t* n);
+int bsf_server_preview_columns(void* s, uint64_t ticket, int32_t* min_y, int32_t* max_y, uint32_t cap);
+int bsf_server_release(void* s, uint64_t ticket); /* frees a finished request's results */
+int bsf_server_get_stats(void* s, bsf_server_stats* out);
+
 /* Allocation-free variant of bsf_chunk_bitmaps. It has no counterpart in the
  * reference: it exists for callers that cannot allocate GPU memory (a host
  * that owns all device memory and passes in pre-allocated buffers, a serving

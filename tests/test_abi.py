@@ -83,3 +83,31 @@ def test_splitmix_matches_oracle():
     for a in (0, 1, 7, 2 ** 40 + 3):
         v = bsf.splitmix_seed(123456789, a)
         assert v & ((1 << 64) - 1) == po.splitmix_seed(123456789, a)
+
+
+def test_config_footprint_sums_the_handle_buffers(lib):
+    small = bsf.config_footprint(capacity=1, centers=1, max_exact_radius=4)
+    big = bsf.config_footprint(capacity=8192)
+    assert 0 < small < big < bsf.config_footprint(capacity=32768)
+    # the state cache grows with capacity, one generator set per world
+    assert bsf.config_footprint(capacity=16384) - big > 8192 * 20000
+    cfg = bsf.Config()
+    lib.bsf_default_config(ctypes.byref(cfg))
+    cfg.max_exact_radius = 25
+    out = ctypes.c_uint64(0)
+    assert lib.bsf_config_footprint(ctypes.byref(cfg), ctypes.byref(out)) == -1
+
+
+def test_server_config_validation_without_a_gpu(lib):
+    cfg = bsf.ServerConfig()
+    lib.bsf_default_server_config(ctypes.byref(cfg))
+    assert (cfg.chunk_worlds, cfg.max_lanes, cfg.max_preview_radius) == (8192, 4, 16)
+    cfg.max_lanes = 0
+    s = lib.bsf_server_open(ctypes.byref(cfg))
+    assert s and b"max_lanes" in lib.bsf_server_last_error(s)
+    t = ctypes.c_uint64(0)
+    seeds = (ctypes.c_int64 * 1)(1)
+    assert lib.bsf_server_submit_range(s, seeds, 1, 7, None, ctypes.byref(t)) == -3  # BSF_E_STATE
+    r = bsf.ServerResult()
+    assert lib.bsf_server_poll(s, 1, 0, ctypes.byref(r)) == -1  # unknown ticket
+    lib.bsf_server_close(s)
