@@ -11,14 +11,22 @@ seeded synthetic consecutive 48-bit values (the full-pipeline workload over
   value  : worlds/s with seeds already resident in HBM (bsf_mega_search_device),
            CUDA events on the stream the kernels run on.
   e2e    : worlds/s through bsf_mega_search with host seeds (H2D + D2H inside).
+  forms  : the plain stage-by-stage form and the served form (bsf.Server: range
+           requests in chunks over several lanes, previews arriving meanwhile)
+           on the same kind of workload, with preview latency alone and mixed.
   --impl reference : the CPU restatement of the reference pipeline (oracle) on
            all host cores, one bounded sample per step.
 Under torchrun each rank takes its own seed range (weak scaling, no collective
 on the data path; a barrier and a max-reduce of the timings only).
 """
+import os
+
+# before any CUDA context: one hardware queue per stream of the served lanes
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import argparse
 import json
-import os
+import math
 import statistics
 import subprocess
 import sys
@@ -45,6 +53,10 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=1024, help="worlds for the CPU baseline sample")
     p.add_argument("--ref-sample", type=int, default=256, help="worlds per reference-arm step")
     p.add_argument("--previews", type=int, default=30)
+    p.add_argument("--served-ranges", type=int, default=4, help="range requests of --batch worlds in the served mix")
+    p.add_argument("--served-chunk", type=int, default=16384, help="worlds per served range chunk (lane capacity)")
+    p.add_argument("--served-lanes", type=int, default=4)
+    p.add_argument("--preview-interval-ms", type=float, default=20.0)
     p.add_argument("--skip-extras", action="store_true")
     return p.parse_args()
 
@@ -234,6 +246,72 @@ def run_reference(args, dist):
     print(json.dumps(line))
 
 
+def served_form(args, bsf, start):
+    """Served mode: range searches and previews through one bsf.Server, previews
+    arriving at a fixed interval while the range requests run. Returns worlds/s
+    over the range requests and preview latency alone and in the mix."""
+    import threading
+    import numpy as np
+    B = args.batch
+    chunk = min(B, args.served_chunk)
+    n_ranges = args.served_ranges
+    blocks = [np.arange(start + i * B, start + (i + 1) * B, dtype=np.int64) for i in range(n_ranges + 1)]
+    pseeds = [int(splitmix(args.seed, 5000 + i) & ((1 << 48) - 1)) for i in range(2 * args.previews + 8)]
+    with bsf.Server(profile=args.profile, chunk_worlds=chunk, max_lanes=args.served_lanes) as srv:
+        # warm-up: open the lanes the mix will use and capture their batch graphs
+        warm = [srv.submit_range(blocks[n_ranges][: chunk * args.served_lanes])]
+        warm += [srv.submit_preview(pseeds[-1 - i], 0, 0, args.radius) for i in range(4)]
+        for t in warm:
+            srv.wait(t, 120)
+            srv.release(t)
+        alone = []
+        for i in range(args.previews):
+            t = srv.submit_preview(pseeds[i], 0, 0, args.radius)
+            alone.append(srv.wait(t, 120).latency_ms)
+            srv.release(t)
+        base = srv.stats()
+        mixed_tickets = []
+        stop = threading.Event()
+
+        def feed():
+            for i in range(args.previews):
+                if stop.is_set():
+                    break
+                mixed_tickets.append(srv.submit_preview(pseeds[args.previews + i], 0, 0, args.radius))
+                time.sleep(args.preview_interval_ms / 1e3)
+
+        t0 = time.perf_counter()
+        rts = [srv.submit_range(blocks[i], radius=args.radius) for i in range(n_ranges)]
+        feeder = threading.Thread(target=feed)
+        feeder.start()
+        for t in rts:
+            r = srv.wait(t, 120)
+            if r.status != 0:
+                raise RuntimeError("served range failed: " + srv.last_error())
+        dt = time.perf_counter() - t0
+        stop.set()
+        feeder.join()
+        mixed = []
+        for t in mixed_tickets:
+            mixed.append(srv.wait(t, 120).latency_ms)
+        st = srv.stats()
+
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))] if v else None
+
+    return {
+        "worlds_per_s": n_ranges * B / dt,
+        "ranges": n_ranges, "worlds_per_range": B, "chunk_worlds": chunk, "lanes": args.served_lanes,
+        "max_busy_lanes": st.max_busy_lanes, "hbm_peak_gb": st.hbm_bytes_peak / 1e9,
+        "hbm_budget_gb": st.hbm_budget / 1e9, "deferred": st.deferred - base.deferred,
+        "preview_alone_ms": {"p50": pct(alone, 0.5), "p99": pct(alone, 0.99), "n": len(alone)},
+        "preview_mixed_ms": {"p50": pct(mixed, 0.5), "p99": pct(mixed, 0.99), "p999": pct(mixed, 0.999),
+                             "n": len(mixed), "interval_ms": args.preview_interval_ms},
+        "radius": args.radius,
+    }
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -320,6 +398,11 @@ def main():
         worker.set_mode(bsf.MODE_QUEUED)
         extras["forms"] = {"queued_worlds_per_s": value / dist.world, "plain_worlds_per_s": plain,
                            "queued_over_plain": (value / dist.world) / plain}
+        if args.served_ranges > 0:
+            served = served_form(args, bsf, seed_start(args.seed, dist.rank, 4))
+            extras["served"] = served
+            extras["forms"]["served_worlds_per_s"] = served["worlds_per_s"]
+            extras["forms"]["served_over_plain"] = served["worlds_per_s"] / plain
         # single-seed island previews (served request class): latency per preview
         lat = []
         for i in range(args.previews):

@@ -13,6 +13,10 @@ import os
 
 import numpy as np
 
+# Served-mode lanes run on separate streams; give each its own hardware queue
+# (must happen before the process creates its CUDA context).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbsf.so")
 WORKER_PATH = os.path.join(HERE, "_build", "bsf_worker")
@@ -72,7 +76,7 @@ class StageCounts(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("profile", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64),
                 ("chunk_worlds", ctypes.c_uint32), ("max_lanes", ctypes.c_int32),
-                ("max_preview_radius", ctypes.c_int32)]
+                ("preview_lanes", ctypes.c_int32), ("max_preview_radius", ctypes.c_int32)]
 
 
 class ServerResult(ctypes.Structure):
@@ -105,7 +109,7 @@ EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
-           "bsf_set_stream_priority", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
+           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
            "bsf_server_records", "bsf_server_preview_columns", "bsf_server_release", "bsf_server_get_stats"]
 
@@ -154,6 +158,7 @@ def load(path=LIB_PATH):
     L.bsf_handle_footprint.argtypes = [vp]
     L.bsf_handle_footprint.restype = ctypes.c_uint64
     L.bsf_set_stream_priority.argtypes = [vp, ctypes.c_int32]
+    L.bsf_set_persistent.argtypes = [vp, ctypes.c_int32]
     L.bsf_default_server_config.argtypes = [P(ServerConfig)]
     L.bsf_server_open.argtypes = [P(ServerConfig)]
     L.bsf_server_open.restype = vp
@@ -271,6 +276,9 @@ class Worker:
         """Device bytes this handle holds."""
         return int(load().bsf_handle_footprint(self._h))
 
+    def set_persistent(self, on=True):
+        self._check(load().bsf_set_persistent(self._h, int(bool(on))))
+
     def set_stream_priority(self, high=True):
         self._check(load().bsf_set_stream_priority(self._h, int(bool(high))))
 
@@ -358,13 +366,14 @@ class Server:
     previews over device-resident lanes, admitted by HBM footprint."""
 
     def __init__(self, profile=PROFILE_MEGA, hbm_budget_bytes=0, chunk_worlds=8192, max_lanes=4,
-                 max_preview_radius=16, device=0):
+                 preview_lanes=2, max_preview_radius=16, device=0):
         L = load()
         cfg = ServerConfig()
         L.bsf_default_server_config(ctypes.byref(cfg))
         cfg.device = device
         cfg.profile = PROFILES.get(profile, profile) if isinstance(profile, str) else profile
         cfg.hbm_budget_bytes, cfg.chunk_worlds, cfg.max_lanes = hbm_budget_bytes, chunk_worlds, max_lanes
+        cfg.preview_lanes = preview_lanes
         cfg.max_preview_radius = max_preview_radius
         self._s = L.bsf_server_open(ctypes.byref(cfg))
         if not self._s:
@@ -421,8 +430,16 @@ class Server:
         st = self._check(load().bsf_server_poll(self._s, ticket, wait_ms, ctypes.byref(r)))
         return None if st == PENDING else r
 
-    def wait(self, ticket):
-        return self.poll(ticket, -1)
+    def wait(self, ticket, timeout_s=600.0):
+        """Block until the ticket finishes; raises BsfError after timeout_s."""
+        import time
+        deadline = time.monotonic() + timeout_s
+        while True:
+            r = self.poll(ticket, 200)
+            if r is not None:
+                return r
+            if time.monotonic() > deadline:
+                raise BsfError("request %d not finished after %.0f s" % (ticket, timeout_s))
 
     def records(self, ticket, cap=1 << 16):
         recs = (MegaRecord * cap)()

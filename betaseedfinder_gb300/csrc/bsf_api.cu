@@ -138,6 +138,7 @@ struct BsfHandle {
     bsf_config cfg{};
     Profile prof{};
     int mode = BSF_MODE_QUEUED;
+    bool persistent = true;  // grid shape of the screened kernels (bsf_set_persistent)
     bool ok = false;
     std::string err;
     cudaStream_t stream = nullptr;
@@ -282,10 +283,10 @@ void record(BsfHandle* h, int i) {
 void run_gpu_stages_queued(BsfHandle* h, int n, bool timed) {
     check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
     launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, h->dCoarseQueue, h->dCounters,
-                       h->capacity * h->centers, h->fs, h->stream);
+                       h->capacity * h->centers, h->fs, h->stream, h->persistent);
     if (timed) record(h, 2);
     launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->fs.stats,
-                             h->stream);
+                             h->stream, h->persistent);
     launch_coarse_cc(h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->dLabels, h->dStats, h->dRegions,
                      h->centers, h->stream);
     if (timed) record(h, 3);
@@ -455,7 +456,7 @@ constexpr int kBatchGraphKernels = 6;
 
 cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
     const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
-    const int variants = get_stage0_fast_variant() * 64 + get_coarse_fast_variant();
+    const int variants = (get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0);
     for (const auto& g : h->graphs)
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
     const unsigned long long launchesBefore = h->launches;
@@ -733,6 +734,13 @@ int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
 uint64_t bsf_handle_footprint(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     return h ? h->footprint : 0;
+}
+
+int bsf_set_persistent(void* hv, int32_t on) {
+    return guarded(hv, [&](BsfHandle* h) {
+        h->persistent = on != 0;
+        return BSF_OK;
+    });
 }
 
 int bsf_set_stream_priority(void* hv, int32_t high) {

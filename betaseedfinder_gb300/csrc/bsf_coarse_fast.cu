@@ -336,10 +336,12 @@ void init_coarse_fast() {
 }
 
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
-                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream) {
+                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream,
+                              bool persistent) {
     if (maxCount <= 0) return;
     const Variant& v = g_variants[g_variant];
-    const int grid = 2 * maxCount < v.grid ? 2 * maxCount : v.grid;
+    // one CTA per half-region of the queue's capacity; CTAs past the device-side count exit at once
+    const int grid = (!persistent || 2 * maxCount < v.grid) ? 2 * maxCount : v.grid;
     v.kernel<<<grid, v.threads, sizeof(CoarseSmem), stream>>>(cache, dQueue, dCount, maxCount, dSigns, stats);
     check(cudaGetLastError(), "k_coarse_signs_fast");
 }

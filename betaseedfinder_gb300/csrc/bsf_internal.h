@@ -116,9 +116,12 @@ struct Stage0FastScratch {
                                           // [2] coarse column tasks, [3] their FP64 fallbacks
 };
 void init_stage0_fast();
+// persistent: one CTA per resident slot looping over worlds (fastest alone);
+// otherwise one CTA per world, so CTAs retire every world and a higher-priority
+// stream's kernels get SM slots without waiting for the whole batch.
 void launch_stage0_fast(const StateCache& cache, int n, int centers, const Profile& prof, RegionInfo* dRegions,
                         RegionRef* dCoarseQueue, int* dCoarseCount, int coarseCapacity, const Stage0FastScratch& fs,
-                        cudaStream_t stream);
+                        cudaStream_t stream, bool persistent = true);
 // Launch-shape variants (threads x CTAs per SM) of the screened kernels, set by the autotuner.
 int stage0_fast_variants();
 const char* stage0_fast_variant_name(int v);
@@ -130,7 +133,8 @@ void set_coarse_fast_variant(int v);
 int get_coarse_fast_variant();
 void init_coarse_fast();
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
-                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream);
+                              std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream,
+                              bool persistent = true);
 // Persistent coarse-score grid for a queue of maxCount regions: label/stat scratch
 // is per CTA (COARSE_CELLS ints of labels, 2 * COARSE_CELLS of stats) and the
 // union-find retry-bound flag (one int) follows the stat scratch.

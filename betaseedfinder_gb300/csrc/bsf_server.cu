@@ -5,12 +5,15 @@
 // and exact-scan scratch) of one request class: RANGE lanes hold chunk_worlds
 // worlds of MEGA pipeline state, PREVIEW lanes one world and exact-scan scratch
 // up to max_preview_radius. Lanes stay open between requests, so generator
-// tables, queues and CUDA graphs are reused. max_lanes worker threads each run
-// one unit of work at a time on a lane: a whole preview, or one chunk of a range
-// request. Previews go first. A unit is admitted when an idle lane of its class
-// exists, or when a new lane's footprint (bsf_config_footprint) fits in the HBM
-// budget, closing idle lanes of the other class if that makes room; otherwise it
-// waits until a lane comes free. Because range requests are handed out a chunk
+// tables, queues and CUDA graphs are reused. max_lanes range worker threads each
+// run one chunk of a range request at a time on a lane, and preview_lanes
+// preview worker threads one preview each, so a preview never waits on the
+// host for a range chunk. On the device, preview lanes use the highest stream
+// priority and range lanes launch their screened kernels one CTA per world, so
+// preview CTAs take SM slots as soon as any world finishes. A unit is admitted
+// when an idle lane of its class exists, or when a new lane's footprint
+// (bsf_config_footprint) fits in the HBM budget, closing idle lanes of the other
+// class if that makes room; otherwise it waits until a lane comes free. Because range requests are handed out a chunk
 // at a time, a request that arrives while others run starts at the next chunk
 // boundary, and the lanes' streams overlap on the device.
 //
@@ -25,6 +28,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -36,6 +40,15 @@
 #include <vector>
 
 namespace {
+
+// The GPU runs the streams of a process on CUDA_DEVICE_MAX_CONNECTIONS hardware
+// queues (8 unless set); streams beyond that share queues, and a kernel then
+// waits for every earlier kernel of any stream on its queue. A preview lane's
+// stream sharing a queue with a range lane's stream would wait for that lane's
+// Stage0 kernel (hundreds of ms under load) however high its priority. The
+// library raises the queue count to the maximum when it is loaded, unless the
+// process set it; it takes effect only if no CUDA context exists yet.
+__attribute__((constructor)) void raise_hardware_queues() { setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0); }
 
 using Clock = std::chrono::steady_clock;
 
@@ -159,10 +172,10 @@ void note_deferred(Server& S, Request* r) {
     }
 }
 
-// Next unit of work, under the lock: previews first, then one chunk of the
+// Next unit of work of one class, under the lock: a preview, or one chunk of the
 // range request at the head of the round robin.
-bool pick(Server& S, Work& w) {
-    if (!S.previews.empty()) {
+bool pick(Server& S, Work& w, int cls) {
+    if (cls == BSF_REQ_PREVIEW && !S.previews.empty()) {
         if (try_lane(S, BSF_REQ_PREVIEW, w)) {
             w.req = S.previews.front();
             S.previews.pop_front();
@@ -170,7 +183,7 @@ bool pick(Server& S, Work& w) {
             note_deferred(S, S.previews.front());
         }
     }
-    if (!w.req && !S.ranges.empty()) {
+    if (cls == BSF_REQ_RANGE && !S.ranges.empty()) {
         if (try_lane(S, BSF_REQ_RANGE, w)) {
             Request* r = S.ranges.front();
             S.ranges.pop_front();
@@ -232,11 +245,18 @@ void run_unit(Server* S, Work& w, int& status, std::string& err, std::vector<bsf
     if (status != BSF_OK) err = lane_error(h, "preview");
 }
 
-void worker_loop(Server* S) {
+// Preview lanes: highest stream priority. Range lanes: one CTA per world in the
+// screened kernels, so they yield SM slots to preview kernels every world.
+void configure_lane(void* h, int kind) {
+    if (kind == BSF_REQ_PREVIEW) bsf_set_stream_priority(h, 1);
+    else bsf_set_persistent(h, 0);
+}
+
+void worker_loop(Server* S, int cls) {
     std::unique_lock<std::mutex> lk(S->mu);
     for (;;) {
         Work w;
-        while (!S->stopping && !pick(*S, w)) S->cvWork.wait(lk);
+        while (!S->stopping && !pick(*S, w, cls)) S->cvWork.wait(lk);
         if (!w.req) return;
         lk.unlock();
         for (void* h : w.evicted) bsf_close(h);
@@ -252,7 +272,7 @@ void worker_loop(Server* S) {
                 if (h) bsf_close(h);
                 laneDead = true;
             } else {
-                if (w.lane->kind == BSF_REQ_PREVIEW) bsf_set_stream_priority(h, 1);
+                configure_lane(h, w.lane->kind);
                 w.lane->h = h;
             }
         }
@@ -357,6 +377,7 @@ void bsf_default_server_config(bsf_server_config* c) {
     c->hbm_budget_bytes = 0;
     c->chunk_worlds = 8192;
     c->max_lanes = 4;
+    c->preview_lanes = 2;
     c->max_preview_radius = 16;
 }
 
@@ -367,8 +388,10 @@ void* bsf_server_open(const bsf_server_config* cfgIn) {
     bsf_default_server_config(&cfg);
     if (cfgIn) cfg = *cfgIn;
     if (cfg.chunk_worlds < 1 || cfg.chunk_worlds > (1u << 20) || cfg.max_lanes < 1 || cfg.max_lanes > 64 ||
-        cfg.max_preview_radius < 1 || cfg.max_preview_radius > 24 || cfg.profile < 0 || cfg.profile > 3) {
-        S->err = "bad server config (chunk_worlds 1..1048576, max_lanes 1..64, max_preview_radius 1..24, profile 0..3)";
+        cfg.preview_lanes < 1 || cfg.preview_lanes > 64 || cfg.max_preview_radius < 1 ||
+        cfg.max_preview_radius > 24 || cfg.profile < 0 || cfg.profile > 3) {
+        S->err = "bad server config (chunk_worlds 1..1048576, max_lanes 1..64, preview_lanes 1..64, "
+                 "max_preview_radius 1..24, profile 0..3)";
         S->stopping = true;
         return S;
     }
@@ -409,7 +432,7 @@ void* bsf_server_open(const bsf_server_config* cfgIn) {
             S->stopping = true;
             return S;
         }
-        if (k == BSF_REQ_PREVIEW) bsf_set_stream_priority(h, 1);
+        configure_lane(h, k);
         auto lane = std::make_unique<Lane>();
         lane->kind = k;
         lane->h = h;
@@ -418,7 +441,8 @@ void* bsf_server_open(const bsf_server_config* cfgIn) {
         S->lanes.push_back(std::move(lane));
     }
     S->bytesPeak = S->bytesInUse;
-    for (int t = 0; t < cfg.max_lanes; ++t) S->workers.emplace_back(worker_loop, S);
+    for (int t = 0; t < cfg.max_lanes; ++t) S->workers.emplace_back(worker_loop, S, BSF_REQ_RANGE);
+    for (int t = 0; t < cfg.preview_lanes; ++t) S->workers.emplace_back(worker_loop, S, BSF_REQ_PREVIEW);
     return S;
 }
 
@@ -461,7 +485,7 @@ int bsf_server_submit_range(void* sv, const int64_t* seeds, uint32_t count, int3
     S->ranges.push_back(r.get());
     S->reqs[r->ticket] = std::move(r);
     ++S->submitted[BSF_REQ_RANGE];
-    S->cvWork.notify_one();
+    S->cvWork.notify_all();  // range and preview workers wait on one condition
     return BSF_OK;
 }
 
@@ -487,7 +511,7 @@ int bsf_server_submit_preview(void* sv, int64_t seed, int32_t cx, int32_t cz, in
     S->previews.push_back(r.get());
     S->reqs[r->ticket] = std::move(r);
     ++S->submitted[BSF_REQ_PREVIEW];
-    S->cvWork.notify_one();
+    S->cvWork.notify_all();  // range and preview workers wait on one condition
     return BSF_OK;
 }
 

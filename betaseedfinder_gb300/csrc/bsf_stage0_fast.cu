@@ -598,11 +598,11 @@ std::size_t stage0_fast_smem() { return sizeof(FastSmem); }
 
 void launch_stage0_fast(const StateCache& cache, int n, int centers, const Profile& prof, RegionInfo* dRegions,
                         RegionRef* dCoarseQueue, int* dCoarseCount, int coarseCapacity, const Stage0FastScratch& fs,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, bool persistent) {
     if (n <= 0) return;
     check(cudaMemsetAsync(fs.p19Count, 0, sizeof(int), stream), "memset");
     const Variant& v = g_variants[g_variant];
-    const int grid = n < v.grid ? n : v.grid;
+    const int grid = (!persistent || n < v.grid) ? n : v.grid;
     v.kernel<<<grid, v.threads, sizeof(FastSmem), stream>>>(cache, n, centers, prof, dRegions, fs);
     check(cudaGetLastError(), "k_stage0_fast");
     const int p19Grid = g_sms;

@@ -162,6 +162,14 @@ int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_vari
  * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
 int bsf_measure_peaks(double* ops_per_s2);
 
+/* Grid shape of the screened Stage0 and coarse kernels. on != 0 (default):
+ * persistent grids, one CTA per resident slot looping over worlds (fastest when
+ * the handle has the GPU to itself). on == 0: one CTA per world (Stage0) and per
+ * half-region of the coarse queue, so CTAs retire every world and kernels of a
+ * higher-priority stream start without waiting for the batch (served mode's
+ * range lanes). Results are identical either way. */
+int bsf_set_persistent(void* h, int32_t on);
+
 /* Device memory (bytes) a handle opened with cfg allocates, computed without a
  * GPU from the same buffer list bsf_open allocates; BSF_E_ARG for a bad config. */
 int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes);
@@ -173,6 +181,10 @@ uint64_t bsf_handle_footprint(const void* h);
 int bsf_set_stream_priority(void* h, int32_t high);
 
 /* ---- Served mode (bsf_server_*) ------------------------------------------
+ * Lanes run on separate streams; for their kernels to overlap without false
+ * dependencies the process needs CUDA_DEVICE_MAX_CONNECTIONS above the number
+ * of lanes. Loading libbsf sets it to 32 unless it is already set, which works
+ * when the library is loaded before the process's first CUDA call.
  * A request loop that keeps generator caches, stage queues and scratch
  * resident on the device in "lanes" (one handle + stream each) and runs two
  * request classes concurrently:
@@ -198,7 +210,8 @@ typedef struct bsf_server_config {
     int32_t profile;             /* BSF_PROFILE_* of range searches */
     uint64_t hbm_budget_bytes;   /* device bytes all lanes may hold; 0 = half the free memory at open */
     uint32_t chunk_worlds;       /* range lane capacity = worlds per chunk (default 8192) */
-    int32_t max_lanes;           /* lanes busy at once = worker threads (default 4) */
+    int32_t max_lanes;           /* range chunks running at once = range worker threads (default 4) */
+    int32_t preview_lanes;       /* previews running at once = preview worker threads (default 2) */
     int32_t max_preview_radius;  /* largest preview radius (default 16, at most 24) */
 } bsf_server_config;
 

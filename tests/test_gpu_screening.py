@@ -102,3 +102,19 @@ def test_batch_graph_replays_match_first_capture():
     assert strip(runs[0][0]) == strip(cp.as_dict()) == strip(cd.as_dict())
     key = lambda rs: [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rs]
     assert runs[0][1] == key(rp) == key(rd)
+
+
+def test_per_world_grids_give_identical_results():
+    """bsf_set_persistent(0) (one CTA per world / half-region, used by served
+    range lanes) changes only the launch shape."""
+    seeds = consecutive(4096, 616)
+    with bsf.Worker(capacity=4096, profile="mega", research=True, centers=8, max_exact_radius=24) as w:
+        a = w.stage0_filter(seeds)
+        ca, ra = w.mega_search(seeds)
+        w.set_persistent(False)
+        b = w.stage0_filter(seeds)
+        cb, rb = w.mega_search(seeds)
+    assert np.array_equal(a, b)
+    assert ca.as_dict() == cb.as_dict()
+    assert [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in ra] == \
+           [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rb]
