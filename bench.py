@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--served-lanes", type=int, default=4)
     p.add_argument("--preview-interval-ms", type=float, default=20.0)
     p.add_argument("--skip-extras", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     return p.parse_args()
 
 
@@ -336,7 +337,7 @@ def main():
     stream = torch.cuda.current_stream(device)
     sptr = stream.cuda_stream
 
-    tune_report = worker.autotune(min(B, 4096))
+    tune_report = "off (default launch shapes)" if args.no_autotune else worker.autotune(min(B, 4096))
     for s in range(W):
         worker.mega_search_device(d_seeds[s].data_ptr(), B, radius=args.radius, stream=sptr)
     torch.cuda.synchronize()

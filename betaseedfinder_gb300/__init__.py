@@ -109,7 +109,7 @@ EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
-           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
+           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
            "bsf_server_records", "bsf_server_preview_columns", "bsf_server_release", "bsf_server_get_stats"]
 
@@ -159,6 +159,7 @@ def load(path=LIB_PATH):
     L.bsf_handle_footprint.restype = ctypes.c_uint64
     L.bsf_set_stream_priority.argtypes = [vp, ctypes.c_int32]
     L.bsf_set_persistent.argtypes = [vp, ctypes.c_int32]
+    L.bsf_set_screening.argtypes = [vp, ctypes.c_int32]
     L.bsf_default_server_config.argtypes = [P(ServerConfig)]
     L.bsf_server_open.argtypes = [P(ServerConfig)]
     L.bsf_server_open.restype = vp
@@ -275,6 +276,10 @@ class Worker:
     def footprint(self):
         """Device bytes this handle holds."""
         return int(load().bsf_handle_footprint(self._h))
+
+    def set_screening(self, on=True):
+        """False: every screened column task takes the exact FP64 fallback path (verification)."""
+        self._check(load().bsf_set_screening(self._h, int(bool(on))))
 
     def set_persistent(self, on=True):
         self._check(load().bsf_set_persistent(self._h, int(bool(on))))

@@ -286,7 +286,7 @@ void run_gpu_stages_queued(BsfHandle* h, int n, bool timed) {
                        h->capacity * h->centers, h->fs, h->stream, h->persistent);
     if (timed) record(h, 2);
     launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->fs.stats,
-                             h->stream, h->persistent);
+                             h->stream, h->persistent, h->fs.forceExact != 0);
     launch_coarse_cc(h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->dLabels, h->dStats, h->dRegions,
                      h->centers, h->stream);
     if (timed) record(h, 3);
@@ -456,7 +456,8 @@ constexpr int kBatchGraphKernels = 6;
 
 cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
     const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
-    const int variants = (get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0);
+    const int variants = ((get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0)) * 2 +
+                         h->fs.forceExact;
     for (const auto& g : h->graphs)
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
     const unsigned long long launchesBefore = h->launches;
@@ -734,6 +735,13 @@ int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
 uint64_t bsf_handle_footprint(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     return h ? h->footprint : 0;
+}
+
+int bsf_set_screening(void* hv, int32_t on) {
+    return guarded(hv, [&](BsfHandle* h) {
+        h->fs.forceExact = on ? 0 : 1;
+        return BSF_OK;
+    });
 }
 
 int bsf_set_persistent(void* hv, int32_t on) {

@@ -10,6 +10,7 @@
 // (bsf_screen.cuh). Undecided columns are recomputed in exact FP64, so the
 // 17-bit sign masks equal those of the FP64 coarse kernel bit for bit.
 #include "bsf_device.cuh"
+#include "bsf_exact_warp.cuh"
 #include "bsf_internal.h"
 #include "bsf_screen.cuh"
 
@@ -103,7 +104,15 @@ __device__ unsigned exact_bits(const CoarseSmem& s, double X, double Z, double d
     return bits;
 }
 
-// Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,17)).
+// Exact FP64 column for Y range r by one whole warp (fallback pass).
+__device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int cz, int r) {
+    if (r == 0) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
+    if (r == 1) return exactwarp::exact_column_warp<6, 6>(s, cx, cz);
+    return exactwarp::exact_column_warp<12, 5>(s, cx, cz);
+}
+
+// Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,17)) by one
+// thread: only when the fallback list of a tile overflows.
 __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int cz, int r) {
     const GenTable t = gtab(s);
     double temp, rain, d5, d7;
@@ -132,46 +141,71 @@ __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int c
 }
 
 // Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds; kx is the half-local row.
+// noise5 first: in the d6 < 0 branch d5 is 0.5 whatever the climate and noise4,
+// which are left out when every converged lane of the warp is in that branch.
 __device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
-    Fe temp, rain;
-    climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
-    float n4 = 0.0f, n5 = 0.0f;
-#pragma unroll
-    for (int o = 0; o < 10; ++o) {
-        const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx), ax_z(s, ST_N4 + o, kz)) *
-                        static_cast<float>(1 << o);
-        n4 = o == 0 ? v : n4 + v;
-    }
+    float n5 = 0.0f;
 #pragma unroll
     for (int o = 0; o < 16; ++o) {
         const float v = octave2f(s.perm + (ST_N5 + o) * PERM_BYTES, ax_x(s, ST_N5 + o, kx), ax_z(s, ST_N5 + o, kz)) *
                         static_cast<float>(1 << o);
         n5 = o == 0 ? v : n5 + v;
     }
-    Fe d5, d7;
-    if (column_shape_f(temp, rain, Fe{n4, E_N4}, Fe{n5, E_N5}, d5, d7)) {
-        sh[0] = d5.v; sh[1] = d5.e; sh[2] = d7.v; sh[3] = d7.e;
-    } else {
-        sh[0] = 0.0f; sh[1] = -1.0f; sh[2] = 0.0f; sh[3] = 0.0f;
+    Fe d5{0.5f, 0.0f}, d7{0.0f, 0.0f};
+    bool zeroD5 = false;
+    const bool decided = shape_d7_f(Fe{n5, E_N5}, d7, zeroD5);
+    zeroD5 = zeroD5 && decided;
+    if (!__all_sync(__activemask(), zeroD5)) {
+        Fe temp, rain;
+        climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
+        float n4 = 0.0f;
+#pragma unroll
+        for (int o = 0; o < 10; ++o) {
+            const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx),
+                                     ax_z(s, ST_N4 + o, kz)) * static_cast<float>(1 << o);
+            n4 = o == 0 ? v : n4 + v;
+        }
+        const Fe d5c = shape_d5_f(temp, rain, Fe{n4, E_N4});
+        d5 = zeroD5 ? Fe{0.5f, 0.0f} : d5c;
     }
+    if (!decided) {
+        sh[0] = 0.0f; sh[1] = -1.0f; sh[2] = 0.0f; sh[3] = 0.0f;
+        return;
+    }
+    sh[0] = d5.v; sh[1] = d5.e; sh[2] = d7.v; sh[3] = d7.e;
 }
 
 template <int Y0, int N>
 __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz, const float* shape, unsigned& bits) {
     if (shape[1] < 0.0f) return false;
     float a1[N], a2[N], a3[N];
-#pragma unroll 1
-    for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, ax_x(s, ST_N2 + o, kx), ax_z(s, ST_N2 + o, kz), s.yf[o],
-                        static_cast<float>(1 << o), a2, o == 0);
-#pragma unroll 1
-    for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, ax_x(s, ST_N3 + o, kx), ax_z(s, ST_N3 + o, kz),
-                        s.yf[16 + o], static_cast<float>(1 << o), a3, o == 0);
+    // noise1 first: per level it selects noise2, noise3 or their lerp
 #pragma unroll 1
     for (int o = 0; o < 8; ++o)
         octave3f<Y0, N>(s.perm + (ST_N1 + o) * PERM_BYTES, ax_x(s, ST_N1 + o, kx), ax_z(s, ST_N1 + o, kz),
                         s.yf[32 + o], static_cast<float>(1 << o), a1, o == 0);
+    unsigned need = 0;
+#pragma unroll
+    for (int k = 0; k < N; ++k) need |= noise_select_f(a1[k]);
+    need = __reduce_or_sync(__activemask(), need);  // warp-uniform: skip a sum no converged lane reads
+    if (need & 1u) {
+#pragma unroll 1
+        for (int o = 0; o < 16; ++o)
+            octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, ax_x(s, ST_N2 + o, kx), ax_z(s, ST_N2 + o, kz),
+                            s.yf[o], static_cast<float>(1 << o), a2, o == 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) a2[k] = 0.0f;  // read by no level
+    }
+    if (need & 2u) {
+#pragma unroll 1
+        for (int o = 0; o < 16; ++o)
+            octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, ax_x(s, ST_N3 + o, kx), ax_z(s, ST_N3 + o, kz),
+                            s.yf[16 + o], static_cast<float>(1 << o), a3, o == 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) a3[k] = 0.0f;  // read by no level
+    }
     const Fe d5{shape[0], shape[1]}, d7{shape[2], shape[3]};
     unsigned b = 0;
 #pragma unroll
@@ -189,7 +223,7 @@ template <int CT, int MINB>
 __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache, const RegionRef* __restrict__ queue,
                                                              const int* count, int maxCount,
                                                              std::uint32_t* __restrict__ signs,
-                                                             unsigned long long* stats) {
+                                                             unsigned long long* stats, int forceExact) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CoarseSmem& s = *reinterpret_cast<CoarseSmem*>(smem_raw);
     const int tid = threadIdx.x;
@@ -257,7 +291,8 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
                 atomicAdd(&s.screened, 1);
                 unsigned bits = 0;
                 bool ok;
-                if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
+                if (forceExact) ok = false;
+                else if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
                 else if (r == 1) ok = screened_range<6, 6>(s, kx, kz, s.shape[c], bits);
                 else ok = screened_range<12, 5>(s, kx, kz, s.shape[c], bits);
                 if (ok) {
@@ -270,12 +305,14 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
                 }
             }
             __syncthreads();
+            // fallbacks: one warp per undecided column task
             const int nfb = min(s.fbCount, FB_CAP);
-            for (int k = tid; k < nfb; k += CT) {
+            for (int k = tid >> 5; k < nfb; k += CT >> 5) {
                 const int e = s.fb[k];
                 const int c = e & 0xFFF, r = e >> 12;
                 const int gg = base + c;
-                atomicOr(&s.mask[c], exact_column(s, originX + row0 + gg / SIDE, originZ + gg % SIDE, r));
+                const unsigned bits = exact_column_w(s, originX + row0 + gg / SIDE, originZ + gg % SIDE, r);
+                if ((tid & 31) == 0) atomicOr(&s.mask[c], bits);
             }
             __syncthreads();
             if (g < cols)
@@ -302,7 +339,7 @@ void check(cudaError_t e, const char* what) {
 struct Variant {
     const char* name;
     int threads;
-    void (*kernel)(StateCache, const RegionRef*, const int*, int, std::uint32_t*, unsigned long long*);
+    void (*kernel)(StateCache, const RegionRef*, const int*, int, std::uint32_t*, unsigned long long*, int);
     int grid;
 };
 Variant g_variants[] = {
@@ -337,12 +374,13 @@ void init_coarse_fast() {
 
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
                               std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream,
-                              bool persistent) {
+                              bool persistent, bool forceExact) {
     if (maxCount <= 0) return;
     const Variant& v = g_variants[g_variant];
     // one CTA per half-region of the queue's capacity; CTAs past the device-side count exit at once
     const int grid = (!persistent || 2 * maxCount < v.grid) ? 2 * maxCount : v.grid;
-    v.kernel<<<grid, v.threads, sizeof(CoarseSmem), stream>>>(cache, dQueue, dCount, maxCount, dSigns, stats);
+    v.kernel<<<grid, v.threads, sizeof(CoarseSmem), stream>>>(cache, dQueue, dCount, maxCount, dSigns, stats,
+                                                              forceExact ? 1 : 0);
     check(cudaGetLastError(), "k_coarse_signs_fast");
 }
 

@@ -274,6 +274,8 @@ struct GenTable {
     }
 };
 
+__device__ __forceinline__ void climate_combine(const double* raw, double& temperature, double& rain);
+
 // Climate at integer block (bx, bz) after normalisation
 // (NoiseGeneratorOctaves2173.java:66-104 octave loop;
 // WorldChunkManager173.java:95-126 formula). The climate generators sit at
@@ -305,6 +307,11 @@ __device__ __forceinline__ void climate_at(const GenTable& t, int bx, int bz, do
         }
         raw[grp] = acc;
     }
+    climate_combine(raw, temperature, rain);
+}
+
+// Temperature and rain from the three raw octave sums (WorldChunkManager173.java:95-126).
+__device__ __forceinline__ void climate_combine(const double* raw, double& temperature, double& rain) {
     const double d0 = raw[2] * 1.1 + 0.5;
     double d1 = 0.01;
     double d2 = 1.0 - d1;

@@ -1,0 +1,125 @@
+// Exact FP64 column evaluated by one warp, for the screened kernels' fallbacks.
+//
+// A screened column task that its error bound cannot decide is recomputed in
+// FP64. Done by one thread, that is ~40 dependent 3D octaves plus the shape:
+// hundreds of microseconds on GB300's FP64 pipe, while the rest of the CTA
+// waits at the next barrier. Every octave term, though, is independent of the
+// others: here each lane computes one or two of them (the 36 shape terms, then
+// the 40 3D octave columns), and the terms are added with warp shuffles in the
+// reference's order (acc = 0.0 + t0, then acc + t1, ...), so every sum, and so
+// every bit, is that of the serial loop (BetaTerrain173.java:739-831,
+// NoiseGeneratorOctaves173.java, NoiseGeneratorOctaves2173.java:66-104).
+//
+// S is the kernel's shared-memory layout; it provides perm, off (the world's
+// generators), yf[40][17] (cell and lattice index per level) and
+// y64[40][17] (FP64 cell fraction and fade per level).
+#pragma once
+
+#include "bsf_device.cuh"
+
+namespace bsf {
+namespace exactwarp {
+
+__device__ __forceinline__ double lane_value(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// The reference's octave accumulation over lanes [first, first + count).
+__device__ __forceinline__ double ordered_sum(double v, int first, int count) {
+    double acc = 0.0 + lane_value(v, first);
+    for (int o = 1; o < count; ++o) acc = acc + lane_value(v, first + o);
+    return acc;
+}
+
+// Shape term i of the column: 0..9 the climate simplex octaves (temperature 4,
+// rain 4, blend 2, each with its weight), 10..19 noise4, 20..35 noise5.
+__device__ __forceinline__ double shape_term(const GenTable& t, int i, double X, double Z, double BX, double BZ) {
+    if (i < 10) {
+        const int grp = i < 4 ? 0 : (i < 8 ? 1 : 2);
+        const int o = i - (grp == 0 ? 0 : (grp == 1 ? 4 : 8));
+        const double scale = grp == 0 ? 0.02500000037252903 : (grp == 1 ? 0.05000000074505806 : 0.25);
+        const double octScale = grp == 0 ? 0.25 : (grp == 1 ? 0.3333333333333333 : 0.5882352941176471);
+        const double d2 = scale / 1.5;
+        double d6 = 1.0, d7 = 1.0;
+        for (int q = 0; q < o; ++q) {  // the serial loop's running products
+            d7 *= octScale;
+            d6 *= 0.5;
+        }
+        const double sx = d2 * d7;
+        const double w = 0.55 / d6;
+        return simplex2(t(ST_TEMP + i), BX * sx, BZ * sx) * w;
+    }
+    const bool n4 = i < 20;
+    const int o = n4 ? i - 10 : i - 20;
+    const double amp = 1.0 / static_cast<double>(1 << o);  // exact, as amp /= 2.0 per octave
+    const double sc = (n4 ? 1.121 : 200.0) * amp;
+    return octave2(t((n4 ? ST_N4 : ST_N5) + o), X * sc, Z * sc) * (1.0 / amp);
+}
+
+// One 3D octave column's terms (octave3_column with the sums left out).
+template <int Y0, int N, typename S>
+__device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int state, int ycol, double sc0, int o,
+                                             double X, double Z, double* out) {
+    const double amp = 1.0 / static_cast<double>(1 << o);
+    const double sc = sc0 * amp;
+    YEntry ya[17];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const int y = Y0 + k;
+        ya[y].cellFrac = s.y64[ycol][y].cellFrac;
+        ya[y].fade = s.y64[ycol][y].fade;
+        ya[y].yi = s.yf[ycol][y].yi;
+        ya[y].cell = s.yf[ycol][y].cell;
+    }
+    double acc[N];
+    octave3_column<Y0, N>(t(state), X * sc, Z * sc, ya, 1.0 / amp, acc, true);
+#pragma unroll
+    for (int k = 0; k < N; ++k) out[k] = acc[k];  // 0.0 + v: the first-octave form, same sum
+}
+
+// Exact density signs of the column at coarse (cx, cz) for levels [Y0, Y0+N),
+// climate sampled at block (4cx+2, 4cz+2). All 32 lanes must call it with the
+// same arguments; every lane returns the same bits.
+template <int Y0, int N, typename S>
+__device__ unsigned exact_column_warp(const S& s, int cx, int cz) {
+    const int lane = threadIdx.x & 31;
+    GenTable t;
+    t.perm = s.perm;
+    t.off = &s.off[0][0];
+    const double X = static_cast<double>(cx), Z = static_cast<double>(cz);
+    const double BX = static_cast<double>(cx * 4 + 2), BZ = static_cast<double>(cz * 4 + 2);
+    // shape: 36 terms over two rounds of lanes
+    const double s0 = shape_term(t, lane, X, Z, BX, BZ);
+    const double s1 = lane < 4 ? shape_term(t, 32 + lane, X, Z, BX, BZ) : 0.0;
+    double raw[3];
+    raw[0] = ordered_sum(s0, 0, 4);
+    raw[1] = ordered_sum(s0, 4, 4);
+    raw[2] = ordered_sum(s0, 8, 2);
+    const double n4 = ordered_sum(s0, 10, 10);
+    double n5 = 0.0 + lane_value(s0, 20);
+    for (int q = 21; q < 32; ++q) n5 = n5 + lane_value(s0, q);
+    for (int q = 0; q < 4; ++q) n5 = n5 + lane_value(s1, q);
+    double temperature, rain;
+    climate_combine(raw, temperature, rain);
+    double d5, d7;
+    column_shape(temperature, rain, n4, n5, d5, d7);
+    // 3D octaves: lanes 0-15 noise2, 16-31 noise3, then lanes 0-7 noise1
+    double tA[N], tB[N];
+    if (lane < 16) octave_terms<Y0, N>(s, t, ST_N2 + lane, lane, NOISE_XZ, lane, X, Z, tA);
+    else octave_terms<Y0, N>(s, t, ST_N3 + lane - 16, lane, NOISE_XZ, lane - 16, X, Z, tA);
+    if (lane < 8) octave_terms<Y0, N>(s, t, ST_N1 + lane, 32 + lane, NOISE_XZ / 80.0, lane, X, Z, tB);
+    else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) tB[k] = 0.0;
+    }
+    unsigned bits = 0;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const double n2 = ordered_sum(tA[k], 0, 16);
+        const double n3 = ordered_sum(tA[k], 16, 16);
+        const double n1 = ordered_sum(tB[k], 0, 8);
+        if (density_at(Y0 + k, d5, d7, n1, n2, n3) > 0.0) bits |= 1u << (Y0 + k);
+    }
+    return bits;
+}
+
+}  // namespace exactwarp
+}  // namespace bsf

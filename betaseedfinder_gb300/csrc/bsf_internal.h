@@ -114,6 +114,7 @@ struct Stage0FastScratch {
     int p19Capacity = 0;
     unsigned long long* stats = nullptr;  // [0] stage0 column tasks, [1] their FP64 fallbacks,
                                           // [2] coarse column tasks, [3] their FP64 fallbacks
+    int forceExact = 0;  // verification: treat every screened column task as undecided
 };
 void init_stage0_fast();
 // persistent: one CTA per resident slot looping over worlds (fastest alone);
@@ -134,7 +135,7 @@ int get_coarse_fast_variant();
 void init_coarse_fast();
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
                               std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream,
-                              bool persistent = true);
+                              bool persistent = true, bool forceExact = false);
 // Persistent coarse-score grid for a queue of maxCount regions: label/stat scratch
 // is per CTA (COARSE_CELLS ints of labels, 2 * COARSE_CELLS of stats) and the
 // union-find retry-bound flag (one int) follows the stat scratch.

@@ -289,16 +289,12 @@ __device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe&
     rain = d4;
 }
 
-// Column shape with bounds (BetaTerrain173.java:753-804). Returns false when
-// the d6 < 0 branch (which zeroes d5) cannot be decided within the bound.
-__device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, Fe& d5out, Fe& d7out) {
-    const Fe d3 = fe_mul(rain, temp);
-    Fe d4 = fe_sub(Fe{1.0f, 0.0f}, d3);
-    d4 = fe_mul(d4, d4);
-    d4 = fe_mul(d4, d4);
-    d4 = fe_sub(Fe{1.0f, 0.0f}, d4);
-    Fe d5 = fe_scale(fe_add(n4, Fe{256.0f, 0.0f}), 1.0f / 512.0f);
-    d5 = fe_clamp_hi(fe_mul(d5, d4), 1.0f);
+// d6 / d7 half of the column shape (BetaTerrain173.java:778-804) from noise5
+// alone. zeroD5 reports the d6 < 0 branch, in which the reference sets d5 to 0
+// before `d5 += 0.5`, so temperature, rain and noise4 cannot change the column
+// there (about 70% of Stage0 columns). Returns false when the branch cannot be
+// decided within the bound.
+__device__ __forceinline__ bool shape_d7_f(Fe n5, Fe& d7out, bool& zeroD5) {
     Fe d6 = fe_div(n5, Fe{8000.0f, 0.0f});
     if (fabsf(d6.v) <= d6.e) {
         d6 = Fe{fabsf(d6.v), d6.e};  // -d6*0.3 and d6 agree at 0: Lipschitz 1
@@ -308,22 +304,55 @@ __device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, F
     }
     d6 = fe_sub(fe_scale(d6, 3.0f), Fe{2.0f, 0.0f});
     if (fabsf(d6.v) <= d6.e) return false;  // d5 = 0 branch undecidable
-    if (d6.v < 0.0f) {
+    zeroD5 = d6.v < 0.0f;
+    if (zeroD5) {
         d6 = fe_scale(d6, 0.5f);
         d6 = fe_clamp_lo(d6, -1.0f);
         d6 = fe_div(d6, Fe{1.4f, 1.4f * U});
         d6 = fe_scale(d6, 0.5f);
-        d5 = Fe{0.0f, 0.0f};
     } else {
         d6 = fe_clamp_hi(d6, 1.0f);
         d6 = fe_scale(d6, 0.125f);
     }
-    d5 = fe_clamp_lo(d5, 0.0f);
-    d5 = fe_add(d5, Fe{0.5f, 0.0f});
     d6 = fe_scale(fe_scale(d6, 17.0f), 1.0f / 16.0f);
-    d5out = d5;
     d7out = fe_add(Fe{8.5f, 0.0f}, fe_scale(d6, 4.0f));
     return true;
+}
+
+// d5 of the d6 >= 0 branch (BetaTerrain173.java:753-777, 801-802): the climate
+// and noise4 term, clamped to [0, 1], plus 0.5.
+__device__ __forceinline__ Fe shape_d5_f(Fe temp, Fe rain, Fe n4) {
+    const Fe d3 = fe_mul(rain, temp);
+    Fe d4 = fe_sub(Fe{1.0f, 0.0f}, d3);
+    d4 = fe_mul(d4, d4);
+    d4 = fe_mul(d4, d4);
+    d4 = fe_sub(Fe{1.0f, 0.0f}, d4);
+    Fe d5 = fe_scale(fe_add(n4, Fe{256.0f, 0.0f}), 1.0f / 512.0f);
+    d5 = fe_clamp_hi(fe_mul(d5, d4), 1.0f);
+    d5 = fe_clamp_lo(d5, 0.0f);
+    return fe_add(d5, Fe{0.5f, 0.0f});
+}
+
+// Whole column shape with bounds (BetaTerrain173.java:753-804); false when the
+// d6 < 0 branch cannot be decided within the bound.
+__device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, Fe& d5out, Fe& d7out) {
+    bool zeroD5 = false;
+    if (!shape_d7_f(n5, d7out, zeroD5)) return false;
+    d5out = zeroD5 ? Fe{0.5f, 0.0f} : shape_d5_f(temp, rain, n4);
+    return true;
+}
+
+// Which of noise2 / noise3 the density at one level reads (BetaTerrain173.java:
+// 812-822): d12 = (n1/10 + 1)/2 selects d10 (noise2) below 0, d11 (noise3) above
+// 1 and their lerp in between. Bit 0: noise2 may be read; bit 1: noise3 may be
+// read. The test is the one density_sign_f applies, on the same FP32 values, so
+// a noise sum that no level reads may be left out (about 57% of Stage0 column
+// tasks need only one of the two 16-octave sums).
+__device__ __forceinline__ unsigned noise_select_f(float n1) {
+    const Fe d12 = fe_scale(fe_add(fe_div(Fe{n1, E_N1}, Fe{10.0f, 0.0f}), Fe{1.0f, 0.0f}), 0.5f);
+    if (d12.v + d12.e < 0.0f) return 1u;
+    if (d12.v - d12.e > 1.0f) return 2u;
+    return 3u;
 }
 
 // Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1

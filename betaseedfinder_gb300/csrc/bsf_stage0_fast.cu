@@ -17,6 +17,7 @@
 // (gpu_p20_benchmark.cpp:1022-1128, p19_monster_gate.hpp:48-79), then the
 // coarse-queue append.
 #include "bsf_device.cuh"
+#include "bsf_exact_warp.cuh"
 #include "bsf_internal.h"
 #include "bsf_screen.cuh"
 
@@ -210,11 +211,12 @@ __device__ __noinline__ bool screened_bits(const FastSmem& s, int c, int col, un
 }
 
 // One column task: screened, else queued for (or, when the list is full, given) the exact path.
-__device__ __forceinline__ void column_task(FastSmem& s, int c, int col, int r, bool store) {
+__device__ __forceinline__ void column_task(FastSmem& s, int c, int col, int r, bool store, bool forceExact) {
     atomicAdd(&s.screened, 1);
     unsigned bits = 0;
     bool ok;
-    if (r == 0) ok = screened_bits<11, 6>(s, c, col, bits);
+    if (forceExact) ok = false;
+    else if (r == 0) ok = screened_bits<11, 6>(s, c, col, bits);
     else if (r == 1) ok = screened_bits<0, 6>(s, c, col, bits);
     else ok = screened_bits<6, 5>(s, c, col, bits);
     if (ok) {
@@ -228,13 +230,24 @@ __device__ __forceinline__ void column_task(FastSmem& s, int c, int col, int r, 
     else atomicOr(&s.mask17[c][col], exact_task(s, c, col, r));
 }
 
+// Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
+__device__ __noinline__ unsigned exact_task_w(const FastSmem& s, int c, int col, int r) {
+    int cx, cz, kx, kz;
+    column_coords(c, col, cx, cz, kx, kz);
+    if (r == 0) return exactwarp::exact_column_warp<11, 6>(s, cx, cz);
+    if (r == 1) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
+    return exactwarp::exact_column_warp<6, 5>(s, cx, cz);
+}
+
+// Fallback pass: one warp per undecided column task.
 __device__ void run_fallbacks(FastSmem& s) {
     __syncthreads();
     const int n = min(s.fbCount, FB_CAP);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int k = threadIdx.x >> 5; k < n; k += blockDim.x >> 5) {
         const std::uint32_t e = s.fb[k];
         const int r = e >> 12, c = (e >> 8) & 15, col = e & 255;
-        atomicOr(&s.mask17[c][col], exact_task(s, c, col, r));
+        const unsigned bits = exact_task_w(s, c, col, r);
+        if ((threadIdx.x & 31) == 0) atomicOr(&s.mask17[c][col], bits);
     }
     __syncthreads();
     if (threadIdx.x == 0) s.fbCount = 0;
@@ -300,7 +313,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         for (int t = tid; t < centers * 64; t += FT) {
             const int c = t >> 6, k = t & 63;
-            column_task(s, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true);
+            column_task(s, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true, fs.forceExact);
         }
         run_fallbacks(s);
         for (int t = tid; t < centers * 64; t += FT) {
@@ -322,7 +335,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
         const int upperCenters = s.taskCount;
         for (int t = tid; t < upperCenters * 192; t += FT)
-            column_task(s, s.tasks[t / 192], cf_nonaxis_cols[t % 192], 0, true);
+            column_task(s, s.tasks[t / 192], cf_nonaxis_cols[t % 192], 0, true, fs.forceExact);
         run_fallbacks(s);
         for (int t = tid; t < upperCenters * 192; t += FT) {
             const int c = s.tasks[t / 192];
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int lowerTasks = s.taskCount * 2;
         for (int t = tid; t < lowerTasks; t += FT) {
             const int e = s.tasks[t >> 1];
-            column_task(s, e >> 8, e & 255, (t & 1) ? 2 : 1, false);
+            column_task(s, e >> 8, e & 255, (t & 1) ? 2 : 1, false, fs.forceExact);
         }
         run_fallbacks(s);
         // Highest re-entry per lower column; the axis arrays serve as the 8x256 byte grid now.

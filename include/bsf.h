@@ -162,6 +162,11 @@ int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_vari
  * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
 int bsf_measure_peaks(double* ops_per_s2);
 
+/* Verification switch for the queued form: on == 0 sends every column task of
+ * the screened Stage0 and coarse kernels down their exact FP64 fallback path
+ * (slow; results must not change). Default on. */
+int bsf_set_screening(void* h, int32_t on);
+
 /* Grid shape of the screened Stage0 and coarse kernels. on != 0 (default):
  * persistent grids, one CTA per resident slot looping over worlds (fastest when
  * the handle has the GPU to itself). on == 0: one CTA per world (Stage0) and per

@@ -118,3 +118,25 @@ def test_per_world_grids_give_identical_results():
     assert ca.as_dict() == cb.as_dict()
     assert [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in ra] == \
            [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rb]
+
+
+def test_exact_fallback_paths_alone_match_fp64():
+    """Screening off: every column task goes down the fallback paths (the
+    warp-cooperative FP64 column and, past the fallback list, the per-thread
+    one) and must give the FP64 kernels' records and MEGA results."""
+    seeds = consecutive(1024, 888)
+    with bsf.Worker(capacity=1024, profile="mega", research=True, centers=8, max_exact_radius=24) as w:
+        w.set_mode(bsf.MODE_PLAIN)
+        exact = w.stage0_filter(seeds)
+        cp, rp = w.mega_search(seeds)
+        w.set_mode(bsf.MODE_QUEUED)
+        w.set_screening(False)
+        forced = w.stage0_filter(seeds)
+        cf, rf = w.mega_search(seeds)
+        w.set_screening(True)
+    assert np.array_equal(forced, exact)
+    strip = lambda c: {k: v for k, v in c.as_dict().items() if k not in ("rng_fallbacks", "screened_tasks", "fallback_tasks")}
+    assert strip(cf) == strip(cp)
+    assert cf.fallback_tasks == cf.screened_tasks > 0
+    assert [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rf] == \
+           [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rp]
