@@ -5,6 +5,7 @@
 #include "bsf_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -14,6 +15,7 @@
 #include <shared_mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace bsf {
@@ -134,6 +136,16 @@ static std::shared_mutex& capture_guard() {
     return m;
 }
 
+// One exact-scan context: a stream, exact-scan scratch and a result slot.
+// Context 0 is the handle's own (its stream, scratch and preview buffers); the
+// others let the batch exact stage resolve several regions at once.
+struct ExactCtx {
+    cudaStream_t stream = nullptr;  // nullptr: the handle's current stream
+    void* base = nullptr;           // scratch allocation (contexts 1..)
+    ExactScratch exact;
+    Island* dIsland = nullptr;
+};
+
 struct BsfHandle {
     bsf_config cfg{};
     Profile prof{};
@@ -142,7 +154,8 @@ struct BsfHandle {
     bool ok = false;
     std::string err;
     cudaStream_t stream = nullptr;
-    unsigned long long launches = 0;
+    std::atomic<unsigned long long> launches{0};
+    std::vector<ExactCtx> ectx;  // exact-scan contexts (0: the handle's own)
     int capacity = 0;
     int centers = 8;
     int coarseCap = 0;
@@ -354,18 +367,24 @@ void read_stage_times(BsfHandle* h) {
     check(cudaEventElapsedTime(&h->stageMs[2], h->ev[2], h->ev[3]), "event time");
 }
 
-Island exact_once(BsfHandle* h, int world, int ccx, int ccz, int radius, const MatchSettings& ms, bool preview) {
-    if (radius > h->exact.maxRadius) throw std::length_error("exact radius exceeds the provisioned max_exact_radius");
-    launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, h->exact, h->dIsland, preview ? h->dPrevMin : nullptr,
-                      preview ? h->dPrevMax : nullptr, h->prevCap, false, h->stream);
+Island exact_once(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, int radius, const MatchSettings& ms,
+                  bool preview) {
+    if (radius > x.exact.maxRadius) throw std::length_error("exact radius exceeds the provisioned max_exact_radius");
+    cudaStream_t st = x.stream ? x.stream : h->stream;
+    launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, x.exact, x.dIsland, preview ? h->dPrevMin : nullptr,
+                      preview ? h->dPrevMax : nullptr, h->prevCap, false, st);
     h->launches += 12;
     Island isl;
-    check(cudaMemcpyAsync(&isl, h->dIsland, sizeof(Island), cudaMemcpyDeviceToHost, h->stream), "island download");
-    check(cudaStreamSynchronize(h->stream), "exact scan");
     int err = 0;
-    d2h(h, &err, h->exact.err, sizeof(int), "err");
+    check(cudaMemcpyAsync(&isl, x.dIsland, sizeof(Island), cudaMemcpyDeviceToHost, st), "island download");
+    check(cudaMemcpyAsync(&err, x.exact.err, sizeof(int), cudaMemcpyDeviceToHost, st), "err");
+    check(cudaStreamSynchronize(st), "exact scan");
     if (err) throw std::runtime_error("exact scan union-find exceeded its retry bound");
     return isl;
+}
+
+Island exact_once(BsfHandle* h, int world, int ccx, int ccz, int radius, const MatchSettings& ms, bool preview) {
+    return exact_once(h, h->ectx[0], world, ccx, ccz, radius, ms, preview);
 }
 
 int compare_island(const Island& a, const Island& b) {
@@ -378,11 +397,11 @@ int compare_island(const Island& a, const Island& b) {
 }
 
 // verifySideBorderMatch (IslandSearchEngine.java:3188-3260).
-bool border_verify(BsfHandle* h, int world, int ccx, int ccz, const MatchSettings& ms, Island& best) {
+bool border_verify(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, const MatchSettings& ms, Island& best) {
     static const int radii[5] = {10, 13, 16, 20, 24};
     for (int r : radii) {
         if (r <= best.radiusUsed) continue;
-        const Island e = exact_once(h, world, ccx, ccz, r, ms, false);
+        const Island e = exact_once(h, x, world, ccx, ccz, r, ms, false);
         if (!e.found) return false;
         best = e;
         if (!best.touchesSide) return true;
@@ -391,15 +410,16 @@ bool border_verify(BsfHandle* h, int world, int ccx, int ccz, const MatchSetting
 }
 
 // processGpuRegionAttempt (IslandSearchEngine.java:1878-1971).
-Island resolve(BsfHandle* h, int world, int ccx, int ccz, int radius, int coarse, const MatchSettings& ms) {
-    Island normal = exact_once(h, world, ccx, ccz, radius, ms, false);
+Island resolve(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, int radius, int coarse,
+              const MatchSettings& ms) {
+    Island normal = exact_once(h, x, world, ccx, ccz, radius, ms, false);
     bool have = normal.found != 0;
-    if (have && normal.touchesSide && radius < 24) have = border_verify(h, world, ccx, ccz, ms, normal);
+    if (have && normal.touchesSide && radius < 24) have = border_verify(h, x, world, ccx, ccz, ms, normal);
     Island match = normal;
     if (radius < 16 && coarse >= 120) {
-        Island hot = exact_once(h, world, ccx, ccz, 16, ms, false);
+        Island hot = exact_once(h, x, world, ccx, ccz, 16, ms, false);
         bool haveHot = hot.found != 0;
-        if (haveHot && hot.touchesSide && hot.radiusUsed < 24) haveHot = border_verify(h, world, ccx, ccz, ms, hot);
+        if (haveHot && hot.touchesSide && hot.radiusUsed < 24) haveHot = border_verify(h, x, world, ccx, ccz, ms, hot);
         if (haveHot && (!have || compare_island(hot, match) > 0)) {
             match = hot;
             have = true;
@@ -460,7 +480,7 @@ cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
                          h->fs.forceExact;
     for (const auto& g : h->graphs)
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
-    const unsigned long long launchesBefore = h->launches;
+    const unsigned long long launchesBefore = h->launches.load();
     cudaGraph_t graph = nullptr;
     std::shared_lock<std::shared_mutex> captureLock(capture_guard());
     check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
@@ -531,11 +551,40 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
                   "region info");
         check(cudaStreamSynchronize(h->stream), "region info");
     }
+    // Exact stage: the regions are independent, so up to ectx.size() of them are
+    // resolved at once, each by a host thread on its own stream and scratch.
+    std::vector<Island> resolved(exactN);
+    const int lanes = std::min<int>(static_cast<int>(h->ectx.size()), exactN);
+    if (lanes <= 1) {
+        for (int k = 0; k < exactN; ++k)
+            resolved[k] = resolve(h, h->ectx[0], ex[k].world, center_chunk_x(ex[k].center),
+                                  center_chunk_z(ex[k].center), radius, info[k].coarse, ms);
+    } else {
+        std::atomic<int> next{0};
+        std::vector<std::string> errors(lanes);
+        auto work = [&](int t) {
+            try {
+                check(cudaSetDevice(h->cfg.device), "cudaSetDevice");
+                for (int k = next.fetch_add(1); k < exactN; k = next.fetch_add(1))
+                    resolved[k] = resolve(h, h->ectx[t], ex[k].world, center_chunk_x(ex[k].center),
+                                          center_chunk_z(ex[k].center), radius, info[k].coarse, ms);
+            } catch (const std::exception& e) {
+                errors[t] = e.what();
+                next.store(exactN);
+            }
+        };
+        std::vector<std::thread> helpers;
+        for (int t = 1; t < lanes; ++t) helpers.emplace_back(work, t);
+        work(0);
+        for (auto& t : helpers) t.join();
+        for (const auto& e : errors)
+            if (!e.empty()) throw std::runtime_error(e);
+    }
     unsigned long long islands = 0;
     uint32_t written = 0;
     for (int k = 0; k < exactN; ++k) {
         const int ccx = center_chunk_x(ex[k].center), ccz = center_chunk_z(ex[k].center);
-        const Island isl = resolve(h, ex[k].world, ccx, ccz, radius, info[k].coarse, ms);
+        const Island& isl = resolved[k];
         if (isl.found) ++islands;
         if (written < recordsCap) {
             bsf_mega_record& r = records[written++];
@@ -618,6 +667,22 @@ void open_buffers(BsfHandle* h, const bsf_config& cfg) {
         check(cudaMemsetAsync(h->exact.err, 0, 64, h->stream), "memset");
     }
     h->alloc(reinterpret_cast<void**>(&h->dIsland), sizeof(Island), "island");
+    // exact-scan contexts: the handle's own, plus three more for batch handles
+    // (capacity >= 1024) so that a batch's exact stage resolves regions at once
+    const int lanes = cfg.capacity >= 1024 ? 4 : 1;
+    h->ectx.assign(lanes, ExactCtx{});
+    h->ectx[0].exact = h->exact;
+    h->ectx[0].dIsland = h->dIsland;
+    for (int t = 1; t < lanes; ++t) {
+        ExactCtx& x = h->ectx[t];
+        h->alloc(&x.base, eb, "exact scratch");
+        h->alloc(reinterpret_cast<void**>(&x.dIsland), sizeof(Island), "island");
+        if (!h->dry) {
+            exact_scratch_carve(x.exact, x.base, cfg.max_exact_radius);
+            check(cudaMemsetAsync(x.exact.err, 0, 64, h->stream), "memset");
+            check(cudaStreamCreateWithFlags(&x.stream, cudaStreamNonBlocking), "stream");
+        }
+    }
     h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
     h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
     h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
@@ -711,6 +776,11 @@ void bsf_close(void* hv) {
         if (p) cudaFree(p);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    for (std::size_t t = 1; t < h->ectx.size(); ++t) {
+        if (h->ectx[t].stream) cudaStreamDestroy(h->ectx[t].stream);
+        if (h->ectx[t].base) cudaFree(h->ectx[t].base);
+        if (h->ectx[t].dIsland) cudaFree(h->ectx[t].dIsland);
+    }
     if (h->hSeeds) cudaFreeHost(h->hSeeds);
     if (h->hOut) cudaFreeHost(h->hOut);
     if (h->hPinned) cudaFreeHost(h->hPinned);
@@ -870,7 +940,7 @@ int bsf_resolve_region(void* hv, int64_t seed, int32_t ccx, int32_t ccz, int32_t
         if (!out || radius < 0) throw std::invalid_argument("bsf_resolve_region: bad out/radius");
         if (h->exact.maxRadius < 24) throw std::length_error("bsf_resolve_region needs max_exact_radius 24");
         const int w = single_world(h, seed);
-        to_island(resolve(h, w, ccx, ccz, radius, coarse, to_ms(s)), out);
+        to_island(resolve(h, h->ectx[0], w, ccx, ccz, radius, coarse, to_ms(s)), out);
         return BSF_OK;
     });
 }
@@ -1022,7 +1092,7 @@ int bsf_measure_peaks(double* ops) {
 
 uint64_t bsf_kernel_launches(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
-    return h ? h->launches : 0;
+    return h ? h->launches.load() : 0;
 }
 
 }  // extern "C"
