@@ -419,14 +419,17 @@ def main():
         ops = stage0_fp64_ops(totals) / K
         fp64_peak, fp32_peak = measured_peaks()
         achieved = ops / (stage0_ms / 1e3)
+        # DRAM bytes per launch of k_stage0_fast from an ncu capture of a smaller batch
+        # (dram__bytes_read.sum + dram__bytes_write.sum per world), scaled to this batch:
+        # the traffic is the per-world generator cache and region records, so it grows
+        # in proportion to the worlds.
         traffic = None
-        tpath = os.path.join(ROOT, "profiles", "stage0_traffic.json")
+        tpath = os.path.join(ROOT, "profiles", "k_stage0_fast_mega_8192worlds.md")
         if os.path.exists(tpath):
-            try:
-                t = json.load(open(tpath))
-                traffic = t.get("bytes_per_world", 0) * B
-            except (ValueError, OSError):
-                traffic = None
+            import re
+            m = re.search(r"traffic_bytes_per_world:\s*(\d+)", open(tpath).read())
+            if m:
+                traffic = int(m.group(1)) * B
         cpu = None
         if not args.skip_extras:
             v, cores, dt, _ = cpu_baseline(args, seed_start(args.seed, 0, 3), args.cpu_sample)
