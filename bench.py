@@ -76,37 +76,43 @@ def seed_start(seed, rank, stream_id):
 
 
 class Dist:
+    """One process per GPU under torchrun (NCCL), or gloo on CPU (BSF_DIST_BACKEND=gloo,
+    used by the multi-process tests). Ranks shard the seed space; the only
+    collectives are the timing barrier and the max/sum reductions."""
+
     def __init__(self):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
+        self.device = "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
+            backend = os.environ.get("BSF_DIST_BACKEND") or ("nccl" if torch.cuda.is_available() else "gloo")
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+                self.device = "cuda"
+            dist.init_process_group(backend)
             self.pg = dist
 
     def barrier(self):
         if self.pg:
             self.pg.barrier()
 
-    def max(self, v):
+    def _reduce(self, v, op):
         if not self.pg:
             return v
         import torch
-        t = torch.tensor([float(v)], device="cuda")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self.device)
+        self.pg.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, v):
+        return self._reduce(v, self.pg.ReduceOp.MAX) if self.pg else v
+
     def sum(self, v):
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([float(v)], device="cuda")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
+        return self._reduce(v, self.pg.ReduceOp.SUM) if self.pg else v
 
     def close(self):
         if self.pg:
