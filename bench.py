@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--served-chunk", type=int, default=16384, help="worlds per served range chunk (lane capacity)")
     p.add_argument("--served-lanes", type=int, default=4)
     p.add_argument("--preview-interval-ms", type=float, default=20.0)
+    p.add_argument("--mix-seconds", type=float, default=15.0, help="length of the Poisson mixed served load")
+    p.add_argument("--mix-load", type=float, default=0.6, help="offered load as a fraction of served capacity")
     p.add_argument("--skip-extras", action="store_true")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     return p.parse_args()
@@ -319,6 +321,68 @@ def served_form(args, bsf, start):
     }
 
 
+def served_mix(args, bsf, start, capacity_wps):
+    """Mixed served load shaped like the served-mode workload, scaled to a bench
+    run: Poisson arrivals; 70% single-seed previews of 1-49 chunks (radius 0-3),
+    25% range searches of log-uniform 2^12-2^16 worlds, 5% MEGA sweeps of 2^17
+    worlds; offered at args.mix_load of the measured served capacity. Reports
+    latency percentiles per class and the worlds/s completed."""
+    import numpy as np
+    rng = np.random.default_rng(args.seed)
+    mean_worlds = 0.25 * (2 ** 16 - 2 ** 12) / np.log(2 ** 4) + 0.05 * 2 ** 17
+    rate = args.mix_load * capacity_wps / mean_worlds  # requests per second
+    reqs, t, base = [], 0.0, start
+    while t < args.mix_seconds:
+        t += rng.exponential(1.0 / rate)
+        u = rng.random()
+        if u < 0.70:
+            reqs.append((t, "preview", int(rng.integers(0, 1 << 48)), int(rng.integers(0, 4))))
+        else:
+            n = int(2 ** rng.uniform(12, 16)) if u < 0.95 else 2 ** 17
+            reqs.append((t, "range" if u < 0.95 else "sweep", base, n))
+            base += n
+    lat = {"preview": [], "range": [], "sweep": []}
+    worlds = 0
+    with bsf.Server(profile=args.profile, chunk_worlds=min(args.batch, args.served_chunk),
+                    max_lanes=args.served_lanes, max_preview_radius=16) as srv:
+        warm = [srv.submit_range(np.arange(base, base + args.served_chunk * args.served_lanes, dtype=np.int64))]
+        warm += [srv.submit_preview(int(rng.integers(0, 1 << 48)), 0, 0, r) for r in range(4)]
+        for tk in warm:
+            srv.wait(tk, 120)
+            srv.release(tk)
+        t0 = time.perf_counter()
+        tickets = []
+        for when, kind, a, b in reqs:
+            delay = when - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            if kind == "preview":
+                tickets.append((kind, 0, srv.submit_preview(a, 0, 0, b)))
+            else:
+                tickets.append((kind, b, srv.submit_range(np.arange(a, a + b, dtype=np.int64), radius=args.radius)))
+        for kind, n, tk in tickets:
+            r = srv.wait(tk, 300)
+            if r.status != 0:
+                raise RuntimeError("served request failed: " + srv.last_error())
+            lat[kind].append(r.latency_ms)
+            worlds += n
+            srv.release(tk)
+        elapsed = time.perf_counter() - t0
+        st = srv.stats()
+
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, max(0, int(math.ceil(q * len(v))) - 1))] if v else None
+
+    return {
+        "offered_load": args.mix_load, "seconds": elapsed, "requests": len(reqs),
+        "worlds_per_s": worlds / elapsed, "hbm_peak_gb": st.hbm_bytes_peak / 1e9, "deferred": st.deferred,
+        "latency_ms": {k: {"n": len(v), "p50": pct(v, 0.5), "p99": pct(v, 0.99), "p999": pct(v, 0.999)}
+                       for k, v in lat.items()},
+        "scaled": "ranges 2^12-2^16 and sweeps 2^17 worlds (the workload's 2^24-2^32 / 2^36 scaled to a bench run)",
+    }
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -410,6 +474,9 @@ def main():
             extras["served"] = served
             extras["forms"]["served_worlds_per_s"] = served["worlds_per_s"]
             extras["forms"]["served_over_plain"] = served["worlds_per_s"] / plain
+            if args.mix_seconds > 0:
+                extras["served_mix"] = served_mix(args, bsf, seed_start(args.seed, dist.rank, 5),
+                                                  served["worlds_per_s"])
         # single-seed island previews (served request class): latency per preview
         lat = []
         for i in range(args.previews):

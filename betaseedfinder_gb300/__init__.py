@@ -109,7 +109,7 @@ EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
-           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
+           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
            "bsf_server_records", "bsf_server_preview_columns", "bsf_server_release", "bsf_server_get_stats"]
 
@@ -166,7 +166,9 @@ def load(path=LIB_PATH):
     L.bsf_server_close.argtypes = [vp]
     L.bsf_server_last_error.argtypes = [vp]
     L.bsf_server_last_error.restype = ctypes.c_char_p
-    L.bsf_server_submit_range.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, P(MatchSettings), u64p]
+    L.bsf_server_submit_range.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, P(MatchSettings),
+                                          u64p]
+    L.bsf_set_profile.argtypes = [vp, ctypes.c_int32]
     L.bsf_server_submit_preview.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                             P(MatchSettings), u64p]
     L.bsf_server_poll.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32, P(ServerResult)]
@@ -276,6 +278,10 @@ class Worker:
     def footprint(self):
         """Device bytes this handle holds."""
         return int(load().bsf_handle_footprint(self._h))
+
+    def set_profile(self, profile):
+        self._check(load().bsf_set_profile(self._h, PROFILES.get(profile, profile) if isinstance(profile, str)
+                                           else profile))
 
     def set_screening(self, on=True):
         """False: every screened column task takes the exact FP64 fallback path (verification)."""
@@ -414,11 +420,12 @@ class Server:
     def last_error(self):
         return load().bsf_server_last_error(self._s).decode()
 
-    def submit_range(self, seeds, radius=7, settings=None):
+    def submit_range(self, seeds, radius=7, settings=None, profile=None):
         seeds = np.ascontiguousarray(seeds, dtype=np.int64)
         t = ctypes.c_uint64(0)
         s = settings or default_match_settings()
-        self._check(load().bsf_server_submit_range(self._s, _p(seeds, ctypes.c_int64), len(seeds), radius,
+        prof = -1 if profile is None else (PROFILES.get(profile, profile) if isinstance(profile, str) else profile)
+        self._check(load().bsf_server_submit_range(self._s, _p(seeds, ctypes.c_int64), len(seeds), radius, prof,
                                                    ctypes.byref(s), ctypes.byref(t)))
         return int(t.value)
 

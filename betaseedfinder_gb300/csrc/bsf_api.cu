@@ -476,8 +476,9 @@ constexpr int kBatchGraphKernels = 6;
 
 cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
     const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
-    const int variants = ((get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0)) * 2 +
-                         h->fs.forceExact;
+    const int variants =
+        (((get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0)) * 2 +
+         h->fs.forceExact) * 4 + h->cfg.profile;  // the profile's gates are kernel parameters of the graph
     for (const auto& g : h->graphs)
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
     const unsigned long long launchesBefore = h->launches.load();
@@ -805,6 +806,15 @@ int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
 uint64_t bsf_handle_footprint(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     return h ? h->footprint : 0;
+}
+
+int bsf_set_profile(void* hv, int32_t profile) {
+    return guarded(hv, [&](BsfHandle* h) {
+        if (profile < 0 || profile > 3) throw std::invalid_argument("profile must be 0..3");
+        h->cfg.profile = profile;
+        h->prof = profile_by_id(profile);
+        return BSF_OK;
+    });
 }
 
 int bsf_set_screening(void* hv, int32_t on) {

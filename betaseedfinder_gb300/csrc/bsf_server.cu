@@ -63,6 +63,7 @@ struct Request {
     int kind = BSF_REQ_RANGE;
     bsf_match_settings ms{};
     std::int32_t radius = 7;
+    std::int32_t profile = BSF_PROFILE_MEGA;  // RANGE: hunt profile of the request
     Clock::time_point submitted{};
     bool started = false;
     bool deferredCounted = false;
@@ -232,8 +233,10 @@ void run_unit(Server* S, Work& w, int& status, std::string& err, std::vector<bsf
     void* h = w.lane->h;
     if (r->kind == BSF_REQ_RANGE) {
         recs.resize(kChunkRecords);
-        status = bsf_mega_search(h, r->seeds.data() + w.begin, w.end - w.begin, r->radius, &r->ms, recs.data(),
-                                 kChunkRecords, &nrec, &counts);
+        status = bsf_set_profile(h, r->profile);
+        if (status == BSF_OK)
+            status = bsf_mega_search(h, r->seeds.data() + w.begin, w.end - w.begin, r->radius, &r->ms, recs.data(),
+                                     kChunkRecords, &nrec, &counts);
         if (status != BSF_OK) err = lane_error(h, "range chunk");
         return;
     }
@@ -465,14 +468,15 @@ const char* bsf_server_last_error(const void* sv) {
     return S ? S->err.c_str() : "null server";
 }
 
-int bsf_server_submit_range(void* sv, const int64_t* seeds, uint32_t count, int32_t radius,
+int bsf_server_submit_range(void* sv, const int64_t* seeds, uint32_t count, int32_t radius, int32_t profile,
                             const bsf_match_settings* ms, uint64_t* ticket) {
     Server* S = static_cast<Server*>(sv);
-    if (!S || !seeds || count == 0 || !ticket) return BSF_E_ARG;
+    if (!S || !seeds || count == 0 || !ticket || profile < -1 || profile > 3) return BSF_E_ARG;
     if (radius < 0 || radius > 24) return BSF_E_LIMIT;
     auto r = std::make_unique<Request>();
     r->kind = BSF_REQ_RANGE;
     r->radius = radius;
+    r->profile = profile < 0 ? S->cfg.profile : profile;
     if (ms) r->ms = *ms;
     else bsf_default_match_settings(&r->ms);
     r->seeds.assign(seeds, seeds + count);

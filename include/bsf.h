@@ -162,6 +162,10 @@ int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_vari
  * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
 int bsf_measure_peaks(double* ops_per_s2);
 
+/* Switches the hunt profile (BSF_PROFILE_*) of later batch calls on this handle
+ * (the worker argv profile, chosen per request instead of per process). */
+int bsf_set_profile(void* h, int32_t profile);
+
 /* Verification switch for the queued form: on == 0 sends every column task of
  * the screened Stage0 and coarse kernels down their exact FP64 fallback path
  * (slow; results must not change). Default on. */
@@ -246,8 +250,9 @@ void bsf_default_server_config(bsf_server_config* cfg);
 void* bsf_server_open(const bsf_server_config* cfg);
 void bsf_server_close(void* s); /* waits for running work; pending requests are dropped */
 const char* bsf_server_last_error(const void* s);
-/* Submit calls copy their inputs and return at once with a ticket. */
-int bsf_server_submit_range(void* s, const int64_t* seeds, uint32_t count, int32_t radius,
+/* Submit calls copy their inputs and return at once with a ticket. profile is a
+ * BSF_PROFILE_* for this range request, or -1 for the server's profile. */
+int bsf_server_submit_range(void* s, const int64_t* seeds, uint32_t count, int32_t radius, int32_t profile,
                             const bsf_match_settings* ms, uint64_t* ticket);
 int bsf_server_submit_preview(void* s, int64_t seed, int32_t center_chunk_x, int32_t center_chunk_z,
                               int32_t radius, const bsf_match_settings* ms, uint64_t* ticket);

@@ -107,7 +107,7 @@ def test_server_config_validation_without_a_gpu(lib):
     assert s and b"max_lanes" in lib.bsf_server_last_error(s)
     t = ctypes.c_uint64(0)
     seeds = (ctypes.c_int64 * 1)(1)
-    assert lib.bsf_server_submit_range(s, seeds, 1, 7, None, ctypes.byref(t)) == -3  # BSF_E_STATE
+    assert lib.bsf_server_submit_range(s, seeds, 1, 7, -1, None, ctypes.byref(t)) == -3  # BSF_E_STATE
     r = bsf.ServerResult()
     assert lib.bsf_server_poll(s, 1, 0, ctypes.byref(r)) == -1  # unknown ticket
     lib.bsf_server_close(s)

@@ -150,3 +150,32 @@ def test_idle_lanes_of_the_other_class_are_evicted_for_room(workload):
     assert got_p == [isl for _, isl, _ in previews[:3]]
     assert st.hbm_bytes_peak <= budget
     assert st.evictions >= 1
+
+
+def test_skewed_range_jobs_with_per_request_profiles_and_radii():
+    """Range jobs of log-uniform lengths, each with its own hunt profile, exact
+    radius and island-volume threshold, all in flight at once: every result equals
+    the direct handle call for that job alone."""
+    rng = np.random.default_rng(4242)
+    jobs = []
+    for j in range(10):
+        n = int(np.exp(rng.uniform(np.log(64), np.log(6000))))
+        start = int(rng.integers(0, 2 ** 48 - n))
+        profile = int(rng.integers(0, 4))
+        radius = int(rng.integers(3, 10))
+        ms = bsf.default_match_settings(min_blocks=int(rng.choice([200, 1000, 3000])), min_columns=20)
+        jobs.append((np.arange(start, start + n, dtype=np.int64), profile, radius, ms))
+    with bsf.Server(profile="mega", chunk_worlds=2048, max_lanes=4) as s:
+        tickets = [s.submit_range(seeds, radius=radius, settings=ms, profile=profile)
+                   for seeds, profile, radius, ms in jobs]
+        served = []
+        for t in tickets:
+            r = s.wait(t, 300)
+            assert r.status == 0, s.last_error()
+            served.append((counts_key(r.counts), rec_key(s.records(t))))
+            s.release(t)
+    with bsf.Worker(capacity=6000, profile="mega", centers=8, max_exact_radius=24) as w:
+        for (seeds, profile, radius, ms), got in zip(jobs, served):
+            w.set_profile(profile)
+            c, r = w.mega_search(seeds, radius=radius, settings=ms)
+            assert got == (counts_key(c), rec_key(r))
