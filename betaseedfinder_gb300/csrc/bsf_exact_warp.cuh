@@ -10,9 +10,9 @@
 // every bit, is that of the serial loop (BetaTerrain173.java:739-831,
 // NoiseGeneratorOctaves173.java, NoiseGeneratorOctaves2173.java:66-104).
 //
-// S is the kernel's shared-memory layout; it provides perm, off (the world's
-// generators), yf[40][17] (cell and lattice index per level) and
-// y64[40][17] (FP64 cell fraction and fade per level).
+// S is the kernel's shared-memory layout; it provides perm and off (the world's
+// generators). The FP64 Y axis of each octave is rebuilt here with the same
+// build_yaxis call the kernels' staging uses, so it is the same bit for bit.
 #pragma once
 
 #include "bsf_device.cuh"
@@ -54,21 +54,24 @@ __device__ __forceinline__ double shape_term(const GenTable& t, int i, double X,
     return octave2(t((n4 ? ST_N4 : ST_N5) + o), X * sc, Z * sc) * (1.0 / amp);
 }
 
+// FP64 Y axis of 3D octave state (0..39): the legacy per-cell Y entries of
+// its 17 levels (noise2/3: y scale 684.412 / 2^k; noise1: 684.412 / 160 / 2^k).
+template <typename S>
+__device__ __forceinline__ void y_entries(const S& s, int state, YEntry* ya) {
+    const int k = state < 16 ? state : (state < 32 ? state - 16 : state - 32);
+    const double amp = 1.0 / static_cast<double>(1 << k);
+    const double sy = state < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
+    build_yaxis(sy, s.off[state][1], ya);
+}
+
 // One 3D octave column's terms (octave3_column with the sums left out).
 template <int Y0, int N, typename S>
-__device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int state, int ycol, double sc0, int o,
-                                             double X, double Z, double* out) {
+__device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int state, double sc0, int o, double X,
+                                             double Z, double* out) {
     const double amp = 1.0 / static_cast<double>(1 << o);
     const double sc = sc0 * amp;
     YEntry ya[17];
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const int y = Y0 + k;
-        ya[y].cellFrac = s.y64[ycol][y].cellFrac;
-        ya[y].fade = s.y64[ycol][y].fade;
-        ya[y].yi = s.yf[ycol][y].yi;
-        ya[y].cell = s.yf[ycol][y].cell;
-    }
+    y_entries(s, state, ya);
     double acc[N];
     octave3_column<Y0, N>(t(state), X * sc, Z * sc, ya, 1.0 / amp, acc, true);
 #pragma unroll
@@ -103,9 +106,9 @@ __device__ unsigned exact_column_warp(const S& s, int cx, int cz) {
     column_shape(temperature, rain, n4, n5, d5, d7);
     // 3D octaves: lanes 0-15 noise2, 16-31 noise3, then lanes 0-7 noise1
     double tA[N], tB[N];
-    if (lane < 16) octave_terms<Y0, N>(s, t, ST_N2 + lane, lane, NOISE_XZ, lane, X, Z, tA);
-    else octave_terms<Y0, N>(s, t, ST_N3 + lane - 16, lane, NOISE_XZ, lane - 16, X, Z, tA);
-    if (lane < 8) octave_terms<Y0, N>(s, t, ST_N1 + lane, 32 + lane, NOISE_XZ / 80.0, lane, X, Z, tB);
+    if (lane < 16) octave_terms<Y0, N>(s, t, ST_N2 + lane, NOISE_XZ, lane, X, Z, tA);
+    else octave_terms<Y0, N>(s, t, ST_N3 + lane - 16, NOISE_XZ, lane - 16, X, Z, tA);
+    if (lane < 8) octave_terms<Y0, N>(s, t, ST_N1 + lane, NOISE_XZ / 80.0, lane, X, Z, tB);
     else {
 #pragma unroll
         for (int k = 0; k < N; ++k) tB[k] = 0.0;

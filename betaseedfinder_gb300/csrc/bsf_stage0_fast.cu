@@ -1,11 +1,12 @@
 // Screened Stage0 (P20 -> Upper -> Lower) and the P19 gate for sm_103a.
 //
-// k_stage0_fast: persistent grid, two 256-thread CTAs per SM, each looping over
-// worlds. Per world the CTA stages in shared memory (~110 KB): the 76
-// generators, the FP32 and FP64 Y axes of the 40 3D octaves, and an axis table
-// holding, for each of the 66 lattice octaves (40 3D + 26 2D), the exact
-// lattice index / fraction / fade of the 46 distinct X and 46 distinct Z coarse
-// coordinates that the 8 region centres use (X = -88..92 step 4). Column tasks
+// k_stage0_fast: persistent grid of one CTA per SM slot, each taking two worlds
+// at a time. Per world the CTA stages in shared memory (~93 KB): the 76
+// generators, the FP32 Y axes of the 40 3D octaves, and an axis table holding,
+// for each of the 66 lattice octaves (40 3D + 26 2D), the exact lattice index /
+// fraction / fade of the 46 distinct X and 46 distinct Z coarse coordinates
+// that the 8 region centres use (X = -88..92 step 4). Each phase's task list
+// spans both worlds, so the rounds of the CTA's threads are fuller. Column tasks
 // run their octaves in FP32 (bsf_screen.cuh); columns whose density signs the
 // error bound cannot decide are recomputed in exact FP64, so every mask and
 // count is bit-identical to the FP64 kernel (bsf_stage0.cu). Regions that pass
@@ -34,7 +35,8 @@ using namespace screen;
 
 constexpr int NAX = 46;      // distinct coarse coordinates per axis over the 8 centres
 constexpr int NOCT = 66;      // 40 3D + 26 2D lattice octaves (state index == octave index)
-constexpr int FB_CAP = 256;   // exact-fallback list entries per phase
+constexpr int PAIR = 2;        // worlds staged per CTA pass (measured: 9% faster than one)
+constexpr int FB_CAP = 512;   // exact-fallback list entries per phase (both worlds)
 
 __constant__ unsigned char cf_axis[8] = {0, 2, 5, 7, 8, 10, 13, 15};
 __constant__ unsigned char cf_nonaxis_cols[192];
@@ -44,26 +46,28 @@ __constant__ short cf_p19_right[BSF_P19_NODE_COUNT];
 __constant__ double cf_p19_value[BSF_P19_NODE_COUNT];
 __constant__ short cf_p19_root[BSF_P19_TREE_COUNT];
 
-struct Y64 {
-    double cellFrac, fade;
-};
-
-struct FastSmem {
+// One world's staged state (16-byte aligned: perm and axf are copied / read as uint4).
+struct alignas(16) WorldSmem {
     std::uint8_t perm[ST_COUNT * PERM_BYTES];
     double off[ST_COUNT][3];
     YF yf[OCT3][17];
-    Y64 y64[OCT3][17];
-    float axf[NOCT][2][NAX];   // FP32 fraction
+    float axf[NOCT][2][NAX];   // FP32 fraction; after Lower, the 8 x 256 highest re-entry bytes
     float axd[NOCT][2][NAX];   // FP32 fade
     std::uint8_t axi[NOCT][2][NAX];  // lattice index & 255
     std::uint32_t mask17[8][256];
-    std::uint16_t tasks[8 * 256];
-    std::uint32_t fb[FB_CAP];
     int p20[8], upper[8], high[8], gate[8];
-    int taskCount, fbCount, screened, fallbacks;
 };
 
-__device__ __forceinline__ GenTable gtab(const FastSmem& s) {
+struct FastSmem {
+    WorldSmem w[PAIR];
+    std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
+    std::uint32_t fb[FB_CAP];             // (range << 13 | slot << 11 | centre << 8 | column)
+    int taskCount, fbCount, screened, fallbacks;
+};
+static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
+              "uint4 copies into perm and out of axf need 16-byte alignment");
+
+__device__ __forceinline__ GenTable gtab(const WorldSmem& s) {
     GenTable t;
     t.perm = s.perm;
     t.off = &s.off[0][0];
@@ -78,7 +82,7 @@ __device__ __forceinline__ double octave_scale(int o) {
     return 200.0 / static_cast<double>(1 << (o - 50));
 }
 
-__device__ __forceinline__ AxisF axis_of(const FastSmem& s, int o, int a, int k) {
+__device__ __forceinline__ AxisF axis_of(const WorldSmem& s, int o, int a, int k) {
     const float f = s.axf[o][a][k];
     return AxisF{f, f - 1.0f, s.axd[o][a][k], s.axi[o][a][k]};
 }
@@ -93,32 +97,25 @@ __device__ __forceinline__ void column_coords(int c, int col, int& cx, int& cz, 
 
 // ---- exact FP64 fallback ----------------------------------------------------
 template <int Y0, int N>
-__device__ void exact_octaves(const FastSmem& s, int base, int ycol, double sc0, double X, double Z, int count,
-                              double* acc) {
+__device__ void exact_octaves(const WorldSmem& s, int base, double sc0, double X, double Z, int count, double* acc) {
     const GenTable t = gtab(s);
     double amp = 1.0;
     for (int o = 0; o < count; ++o) {
         const Gen g = t(base + o);
         const double sc = sc0 * amp;
         YEntry ya[17];
-        for (int k = 0; k < N; ++k) {
-            const int y = Y0 + k;
-            ya[y].cellFrac = s.y64[ycol + o][y].cellFrac;
-            ya[y].fade = s.y64[ycol + o][y].fade;
-            ya[y].yi = s.yf[ycol + o][y].yi;
-            ya[y].cell = s.yf[ycol + o][y].cell;
-        }
+        exactwarp::y_entries(s, base + o, ya);
         octave3_column<Y0, N>(g, X * sc, Z * sc, ya, 1.0 / amp, acc, o == 0);
         amp /= 2.0;
     }
 }
 
 template <int Y0, int N>
-__device__ unsigned exact_bits(const FastSmem& s, double X, double Z, double d5, double d7) {
+__device__ unsigned exact_bits(const WorldSmem& s, double X, double Z, double d5, double d7) {
     double a1[N], a2[N], a3[N];
-    exact_octaves<Y0, N>(s, ST_N2, 0, NOISE_XZ, X, Z, 16, a2);
-    exact_octaves<Y0, N>(s, ST_N3, 16, NOISE_XZ, X, Z, 16, a3);
-    exact_octaves<Y0, N>(s, ST_N1, 32, NOISE_XZ / 80.0, X, Z, 8, a1);
+    exact_octaves<Y0, N>(s, ST_N2, NOISE_XZ, X, Z, 16, a2);
+    exact_octaves<Y0, N>(s, ST_N3, NOISE_XZ, X, Z, 16, a3);
+    exact_octaves<Y0, N>(s, ST_N1, NOISE_XZ / 80.0, X, Z, 8, a1);
     unsigned bits = 0;
 #pragma unroll
     for (int k = 0; k < N; ++k)
@@ -127,7 +124,7 @@ __device__ unsigned exact_bits(const FastSmem& s, double X, double Z, double d5,
 }
 
 // Exact column for Y range id r: 0 -> [11,17), 1 -> [0,6), 2 -> [6,11).
-__device__ __noinline__ unsigned exact_task(const FastSmem& s, int c, int col, int r) {
+__device__ __noinline__ unsigned exact_task(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     const GenTable t = gtab(s);
@@ -158,7 +155,7 @@ __device__ __noinline__ unsigned exact_task(const FastSmem& s, int c, int col, i
 
 // ---- screened FP32 path ---------------------------------------------------
 // Column shape (climate + noise4/5); returns false when the d5 branch is undecided.
-__device__ __noinline__ bool screened_shape(const FastSmem& s, int c, int col, Fe& d5, Fe& d7) {
+__device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, Fe& d5, Fe& d7) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     Fe temp, rain;
@@ -181,7 +178,7 @@ __device__ __noinline__ bool screened_shape(const FastSmem& s, int c, int col, F
 
 // Screened signs of one column for levels [Y0, Y0+N); false when undecided.
 template <int Y0, int N>
-__device__ __noinline__ bool screened_bits(const FastSmem& s, int c, int col, unsigned& bits) {
+__device__ __noinline__ bool screened_bits(const WorldSmem& s, int c, int col, unsigned& bits) {
     Fe d5, d7;
     if (!screened_shape(s, c, col, d5, d7)) return false;
     int cx, cz, kx, kz;
@@ -210,28 +207,30 @@ __device__ __noinline__ bool screened_bits(const FastSmem& s, int c, int col, un
     return true;
 }
 
-// One column task: screened, else queued for (or, when the list is full, given) the exact path.
-__device__ __forceinline__ void column_task(FastSmem& s, int c, int col, int r, bool store, bool forceExact) {
+// One column task of world slot q: screened, else queued for (or, when the list
+// is full, given) the exact path.
+__device__ __forceinline__ void column_task(FastSmem& s, int q, int c, int col, int r, bool store, bool forceExact) {
+    WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 1);
     unsigned bits = 0;
     bool ok;
     if (forceExact) ok = false;
-    else if (r == 0) ok = screened_bits<11, 6>(s, c, col, bits);
-    else if (r == 1) ok = screened_bits<0, 6>(s, c, col, bits);
-    else ok = screened_bits<6, 5>(s, c, col, bits);
+    else if (r == 0) ok = screened_bits<11, 6>(w, c, col, bits);
+    else if (r == 1) ok = screened_bits<0, 6>(w, c, col, bits);
+    else ok = screened_bits<6, 5>(w, c, col, bits);
     if (ok) {
-        if (store) s.mask17[c][col] = bits;
-        else if (bits) atomicOr(&s.mask17[c][col], bits);
+        if (store) w.mask17[c][col] = bits;
+        else if (bits) atomicOr(&w.mask17[c][col], bits);
         return;
     }
     atomicAdd(&s.fallbacks, 1);
     const int slot = atomicAdd(&s.fbCount, 1);
-    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 12) | (c << 8) | col);
-    else atomicOr(&s.mask17[c][col], exact_task(s, c, col, r));
+    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
+    else atomicOr(&w.mask17[c][col], exact_task(w, c, col, r));
 }
 
 // Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
-__device__ __noinline__ unsigned exact_task_w(const FastSmem& s, int c, int col, int r) {
+__device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     if (r == 0) return exactwarp::exact_column_warp<11, 6>(s, cx, cz);
@@ -245,9 +244,9 @@ __device__ void run_fallbacks(FastSmem& s) {
     const int n = min(s.fbCount, FB_CAP);
     for (int k = threadIdx.x >> 5; k < n; k += blockDim.x >> 5) {
         const std::uint32_t e = s.fb[k];
-        const int r = e >> 12, c = (e >> 8) & 15, col = e & 255;
-        const unsigned bits = exact_task_w(s, c, col, r);
-        if ((threadIdx.x & 31) == 0) atomicOr(&s.mask17[c][col], bits);
+        const int r = e >> 13, q = (e >> 11) & 1, c = (e >> 8) & 7, col = e & 255;
+        const unsigned bits = exact_task_w(s.w[q], c, col, r);
+        if ((threadIdx.x & 31) == 0) atomicOr(&s.w[q].mask17[c][col], bits);
     }
     __syncthreads();
     if (threadIdx.x == 0) s.fbCount = 0;
@@ -270,6 +269,7 @@ __device__ __forceinline__ int highest_reentry(std::uint32_t mask) {
 }
 
 // FT threads per CTA, MINB CTAs per SM: launch shapes chosen by the autotuner.
+// Each pass stages PAIR worlds; every phase's task list covers both, slot-major.
 template <int FT, int MINB>
 __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int n, int centers, Profile prof,
                                                           RegionInfo* __restrict__ regions, Stage0FastScratch fs) {
@@ -277,78 +277,98 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     FastSmem& s = *reinterpret_cast<FastSmem*>(smem_raw);
     const int tid = threadIdx.x;
     if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
-    for (int world = blockIdx.x; world < n; world += gridDim.x) {
+    for (int pair = blockIdx.x; pair * PAIR < n; pair += gridDim.x) {
+        const int w0 = pair * PAIR;
+        const int nw = min(PAIR, n - w0);
         __syncthreads();
-        {
-            const uint4* src = reinterpret_cast<const uint4*>(cache.perms + static_cast<std::size_t>(world) * WORLD_PERM_BYTES);
-            uint4* dst = reinterpret_cast<uint4*>(s.perm);
+        for (int q = 0; q < nw; ++q) {
+            const uint4* src =
+                reinterpret_cast<const uint4*>(cache.perms + static_cast<std::size_t>(w0 + q) * WORLD_PERM_BYTES);
+            uint4* dst = reinterpret_cast<uint4*>(s.w[q].perm);
             for (int k = tid; k < WORLD_PERM_BYTES / 16; k += FT) dst[k] = src[k];
-            const double* o = cache.offsets + static_cast<std::size_t>(world) * WORLD_OFFSETS;
-            for (int k = tid; k < ST_COUNT * 3; k += FT) s.off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
+            const double* o = cache.offsets + static_cast<std::size_t>(w0 + q) * WORLD_OFFSETS;
+            for (int k = tid; k < ST_COUNT * 3; k += FT) s.w[q].off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
         }
-        if (tid < 8) { s.p20[tid] = 0; s.upper[tid] = 0; s.high[tid] = 0; }
+        if (tid < 8 * nw) {
+            WorldSmem& w = s.w[tid >> 3];
+            const int c = tid & 7;
+            w.p20[c] = 0; w.upper[c] = 0; w.high[c] = 0; w.gate[c] = 0;
+        }
         if (tid == 0) { s.fbCount = 0; s.taskCount = 0; }
-        for (int k = tid; k < 8 * 256; k += FT) (&s.mask17[0][0])[k] = 0;
+        for (int k = tid; k < nw * 8 * 256; k += FT) (&s.w[k >> 11].mask17[0][0])[k & 2047] = 0;
         __syncthreads();
-        if (tid < OCT3) {
-            const int o = tid;
+        if (tid < OCT3 * nw) {
+            const int q = tid / OCT3, o = tid % OCT3;
             const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
             const double amp = 1.0 / static_cast<double>(1 << k);
             const double sy = o < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
             YEntry ya[17];
-            build_yaxis(sy, s.off[o][1], ya);
-            build_yf(ya, s.yf[o]);
-            for (int y = 0; y < 17; ++y) s.y64[o][y] = Y64{ya[y].cellFrac, ya[y].fade};
+            build_yaxis(sy, s.w[q].off[o][1], ya);
+            build_yf(ya, s.w[q].yf[o]);
         }
-        for (int e = tid; e < NOCT * 2 * NAX; e += FT) {
-            const int o = e / (2 * NAX), a = (e / NAX) & 1, k = e % NAX;
+        constexpr int AXES = NOCT * 2 * NAX;
+        for (int e = tid; e < nw * AXES; e += FT) {
+            WorldSmem& w = s.w[e / AXES];
+            const int f = e % AXES;
+            const int o = f / (2 * NAX), a = (f / NAX) & 1, k = f % NAX;
             const double coord = static_cast<double>(-88 + 4 * k);
-            const AxisF ax = make_axis(coord * octave_scale(o), s.off[o][a == 0 ? 0 : 2]);
-            s.axf[o][a][k] = ax.f;
-            s.axd[o][a][k] = ax.fd;
-            s.axi[o][a][k] = static_cast<std::uint8_t>(ax.i);
+            const AxisF ax = make_axis(coord * octave_scale(o), w.off[o][a == 0 ? 0 : 2]);
+            w.axf[o][a][k] = ax.f;
+            w.axd[o][a][k] = ax.fd;
+            w.axi[o][a][k] = static_cast<std::uint8_t>(ax.i);
         }
         __syncthreads();
 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
-        for (int t = tid; t < centers * 64; t += FT) {
-            const int c = t >> 6, k = t & 63;
-            column_task(s, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true, fs.forceExact);
+        const int p20Tasks = centers * 64;
+        for (int t = tid; t < nw * p20Tasks; t += FT) {
+            const int q = t / p20Tasks, u = t % p20Tasks;
+            const int c = u >> 6, k = u & 63;
+            column_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true, fs.forceExact);
         }
         run_fallbacks(s);
-        for (int t = tid; t < centers * 64; t += FT) {
-            const int c = t >> 6, k = t & 63;
-            if (s.mask17[c][cf_axis[k >> 3] * 16 + cf_axis[k & 7]]) atomicAdd(&s.p20[c], 1);
+        for (int t = tid; t < nw * p20Tasks; t += FT) {
+            const int q = t / p20Tasks, u = t % p20Tasks;
+            const int c = u >> 6, k = u & 63;
+            if (s.w[q].mask17[c][cf_axis[k >> 3] * 16 + cf_axis[k & 7]]) atomicAdd(&s.w[q].p20[c], 1);
         }
         __syncthreads();
         if (tid == 0) {
             int nt = 0;
-            for (int c = 0; c < centers; ++c) {
-                const int g = prof.p20MinCount > 1 ? (s.p20[c] >= prof.p20MinCount ? s.p20[c] : 0) : s.p20[c];
-                s.gate[c] = g;
-                s.upper[c] = g;  // fullUpperCount starts from the gated P20 count (p33_shared_y.hpp:164)
-                if (g > 0) s.tasks[nt++] = static_cast<std::uint16_t>(c);
+            for (int q = 0; q < nw; ++q) {
+                WorldSmem& w = s.w[q];
+                for (int c = 0; c < centers; ++c) {
+                    const int g = prof.p20MinCount > 1 ? (w.p20[c] >= prof.p20MinCount ? w.p20[c] : 0) : w.p20[c];
+                    w.gate[c] = g;
+                    w.upper[c] = g;  // fullUpperCount starts from the gated P20 count (p33_shared_y.hpp:164)
+                    if (g > 0) s.tasks[nt++] = static_cast<std::uint16_t>((q << 3) | c);
+                }
             }
             s.taskCount = nt;
         }
         __syncthreads();
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
-        const int upperCenters = s.taskCount;
-        for (int t = tid; t < upperCenters * 192; t += FT)
-            column_task(s, s.tasks[t / 192], cf_nonaxis_cols[t % 192], 0, true, fs.forceExact);
+        const int upperUnits = s.taskCount;
+        for (int t = tid; t < upperUnits * 192; t += FT) {
+            const int e = s.tasks[t / 192];
+            column_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], 0, true, fs.forceExact);
+        }
         run_fallbacks(s);
-        for (int t = tid; t < upperCenters * 192; t += FT) {
-            const int c = s.tasks[t / 192];
-            if (s.mask17[c][cf_nonaxis_cols[t % 192]]) atomicAdd(&s.upper[c], 1);
+        for (int t = tid; t < upperUnits * 192; t += FT) {
+            const int e = s.tasks[t / 192];
+            if (s.w[e >> 3].mask17[e & 7][cf_nonaxis_cols[t % 192]]) atomicAdd(&s.w[e >> 3].upper[e & 7], 1);
         }
         __syncthreads();
         if (tid == 0) s.taskCount = 0;
         __syncthreads();
-        for (int t = tid; t < centers * 256; t += FT) {
-            const int c = t >> 8, col = t & 255;
-            if (s.gate[c] > 0 && s.upper[c] >= prof.upperMinCount && s.mask17[c][col] != 0) {
+        const int allCols = centers * 256;
+        for (int t = tid; t < nw * allCols; t += FT) {
+            const int q = t / allCols, u = t % allCols;
+            const int c = u >> 8, col = u & 255;
+            const WorldSmem& w = s.w[q];
+            if (w.gate[c] > 0 && w.upper[c] >= prof.upperMinCount && w.mask17[c][col] != 0) {
                 const int slot = atomicAdd(&s.taskCount, 1);
-                s.tasks[slot] = static_cast<std::uint16_t>((c << 8) | col);
+                s.tasks[slot] = static_cast<std::uint16_t>((q << 11) | (c << 8) | col);
             }
         }
         __syncthreads();
@@ -356,48 +376,50 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int lowerTasks = s.taskCount * 2;
         for (int t = tid; t < lowerTasks; t += FT) {
             const int e = s.tasks[t >> 1];
-            column_task(s, e >> 8, e & 255, (t & 1) ? 2 : 1, false, fs.forceExact);
+            column_task(s, e >> 11, (e >> 8) & 7, e & 255, (t & 1) ? 2 : 1, false, fs.forceExact);
         }
         run_fallbacks(s);
-        // Highest re-entry per lower column; the axis arrays serve as the 8x256 byte grid now.
-        std::uint8_t* highest = reinterpret_cast<std::uint8_t*>(&s.axf[0][0][0]);
-        for (int k = tid; k < 8 * 256; k += FT) highest[k] = 0xFF;
+        // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
+        for (int k = tid; k < nw * 8 * 256; k += FT)
+            reinterpret_cast<std::uint8_t*>(&s.w[k >> 11].axf[0][0][0])[k & 2047] = 0xFF;
         __syncthreads();
         for (int t = tid; t < s.taskCount; t += FT) {
             const int e = s.tasks[t];
-            const int c = e >> 8, col = e & 255;
-            const int h = highest_reentry(s.mask17[c][col]);
-            highest[c * 256 + col] = h < 0 ? 0xFF : static_cast<std::uint8_t>(h);
-            if (h >= 11) atomicAdd(&s.high[c], 1);
+            const int q = e >> 11, c = (e >> 8) & 7, col = e & 255;
+            WorldSmem& w = s.w[q];
+            const int h = highest_reentry(w.mask17[c][col]);
+            reinterpret_cast<std::uint8_t*>(&w.axf[0][0][0])[c * 256 + col] = h < 0 ? 0xFF : static_cast<std::uint8_t>(h);
+            if (h >= 11) atomicAdd(&w.high[c], 1);
         }
         __syncthreads();
-        // Region outcomes; P19 candidates go to the P19 queue with their grids.
-        for (int c = 0; c < centers; ++c) {
-            const bool eval = s.p20[c] >= prof.p20MinCount && s.upper[c] >= prof.upperMinCount &&
-                              s.high[c] >= prof.highMinCount;
-            __shared__ int slotShared;
-            if (tid == 0) {
+        // Region outcomes, one warp per (world, centre); P19 candidates go to the P19 queue with their grids.
+        const int warp = tid >> 5, lane = tid & 31;
+        for (int u = warp; u < nw * centers; u += FT / 32) {
+            const int q = u / centers, c = u % centers;
+            const WorldSmem& w = s.w[q];
+            const bool eval = w.p20[c] >= prof.p20MinCount && w.upper[c] >= prof.upperMinCount &&
+                              w.high[c] >= prof.highMinCount;
+            int slot = -1;
+            if (lane == 0) {
                 RegionInfo r;
                 r.p19Score = __longlong_as_double(0x7ff8000000000000LL);
                 r.coarse = 0;
-                r.p20 = static_cast<std::int16_t>(s.p20[c]);
-                r.upper = static_cast<std::int16_t>(s.upper[c]);
-                r.high = static_cast<std::int16_t>(s.high[c]);
+                r.p20 = static_cast<std::int16_t>(w.p20[c]);
+                r.upper = static_cast<std::int16_t>(w.upper[c]);
+                r.high = static_cast<std::int16_t>(w.high[c]);
                 r.p19Evaluated = r.p19Pass = r.p19Extreme = r.megaReject = r.coarseEvaluated = r.pad0 = 0;
                 r.fullY88 = r.fullY96 = r.fullY104 = r.fullY112 = r.y88Largest = r.y96Largest = 0;
                 r.y88Width = r.y88Depth = r.y88Touches = r.y96Width = r.y96Depth = r.y96Touches = 0;
                 r.pad1[0] = r.pad1[1] = 0;
-                regions[static_cast<std::size_t>(world) * centers + c] = r;
-                slotShared = eval ? atomicAdd(fs.p19Count, 1) : -1;
-                if (eval && slotShared < fs.p19Capacity) fs.p19Queue[slotShared] = RegionRef{world, c};
+                regions[static_cast<std::size_t>(w0 + q) * centers + c] = r;
+                slot = eval ? atomicAdd(fs.p19Count, 1) : -1;
+                if (eval && slot < fs.p19Capacity) fs.p19Queue[slot] = RegionRef{w0 + q, c};
             }
-            __syncthreads();
-            const int slot = slotShared;
-            if (slot >= 0 && slot < fs.p19Capacity && tid < 16) {
-                const uint4* src = reinterpret_cast<const uint4*>(highest + c * 256);
-                reinterpret_cast<uint4*>(fs.highest + static_cast<std::size_t>(slot) * 256)[tid] = src[tid];
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (slot >= 0 && slot < fs.p19Capacity && lane < 16) {
+                const uint4* src = reinterpret_cast<const uint4*>(&w.axf[0][0][0]) + c * 16;
+                reinterpret_cast<uint4*>(fs.highest + static_cast<std::size_t>(slot) * 256)[lane] = src[lane];
             }
-            __syncthreads();
         }
     }
     __syncthreads();
@@ -615,7 +637,8 @@ void launch_stage0_fast(const StateCache& cache, int n, int centers, const Profi
     if (n <= 0) return;
     check(cudaMemsetAsync(fs.p19Count, 0, sizeof(int), stream), "memset");
     const Variant& v = g_variants[g_variant];
-    const int grid = (!persistent || n < v.grid) ? n : v.grid;
+    const int pairs = (n + PAIR - 1) / PAIR;  // a CTA takes PAIR worlds per pass
+    const int grid = (!persistent || pairs < v.grid) ? pairs : v.grid;
     v.kernel<<<grid, v.threads, sizeof(FastSmem), stream>>>(cache, n, centers, prof, dRegions, fs);
     check(cudaGetLastError(), "k_stage0_fast");
     const int p19Grid = g_sms;
