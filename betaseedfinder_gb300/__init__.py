@@ -60,7 +60,9 @@ class MegaRecord(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_int64), ("world_index", ctypes.c_int32), ("center_index", ctypes.c_int32),
                 ("center_chunk_x", ctypes.c_int32), ("center_chunk_z", ctypes.c_int32),
                 ("p20", ctypes.c_int32), ("upper", ctypes.c_int32), ("high", ctypes.c_int32),
-                ("coarse", ctypes.c_int32), ("p19_score", ctypes.c_double), ("island", Island)]
+                ("coarse", ctypes.c_int32), ("p19_score", ctypes.c_double), ("island", Island),
+                ("raw_island", Island), ("hot_island", Island), ("hot_scanned", ctypes.c_int32),
+                ("final_source", ctypes.c_int32), ("p19_pass", ctypes.c_int32), ("p19_extreme", ctypes.c_int32)]
 
 
 class StageCounts(ctypes.Structure):

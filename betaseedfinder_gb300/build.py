@@ -71,9 +71,9 @@ def build(verbose=False, extra_flags=()):
         subprocess.check_call([cc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", tmp, *objs,
                                "-lcudart", "-lpthread"])
         os.replace(tmp, LIB)
-    wsrc = os.path.join(CSRC, "bsf_worker.cpp")
-    if _stale(WORKER, [wsrc, LIB, os.path.join(ROOT, "include", "bsf.h")]):
-        subprocess.check_call(["g++", "-std=c++17", "-O2", "-o", WORKER, wsrc, "-L" + BUILD, "-lbsf",
+    wsrc = [os.path.join(CSRC, "bsf_worker.cpp"), os.path.join(CSRC, "bsf_hunt.cpp")]
+    if _stale(WORKER, wsrc + [LIB, os.path.join(ROOT, "include", "bsf.h")]):
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-o", WORKER, *wsrc, "-L" + BUILD, "-lbsf",
                                "-Wl,-rpath,$ORIGIN"])
     return LIB
 

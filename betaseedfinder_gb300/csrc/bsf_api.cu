@@ -409,22 +409,40 @@ bool border_verify(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, const
     return true;
 }
 
+// The steps of one region's resolution, for the candidate log.
+struct ResolveDetail {
+    Island raw{}, hot{};  // found == 0: none (raw after border verify; hot after border verify)
+    bool hotScanned = false;
+    int finalSource = 0;  // 0 none, 1 raw, 2 hot
+};
+
 // processGpuRegionAttempt (IslandSearchEngine.java:1878-1971).
 Island resolve(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, int radius, int coarse,
-              const MatchSettings& ms) {
+              const MatchSettings& ms, ResolveDetail* detail = nullptr) {
     Island normal = exact_once(h, x, world, ccx, ccz, radius, ms, false);
     bool have = normal.found != 0;
     if (have && normal.touchesSide && radius < 24) have = border_verify(h, x, world, ccx, ccz, ms, normal);
     Island match = normal;
+    int source = have ? 1 : 0;
+    if (detail) {
+        detail->raw = have ? normal : Island{};
+        detail->hot = Island{};
+    }
     if (radius < 16 && coarse >= 120) {
         Island hot = exact_once(h, x, world, ccx, ccz, 16, ms, false);
         bool haveHot = hot.found != 0;
         if (haveHot && hot.touchesSide && hot.radiusUsed < 24) haveHot = border_verify(h, x, world, ccx, ccz, ms, hot);
+        if (detail) {
+            detail->hotScanned = true;
+            if (haveHot) detail->hot = hot;
+        }
         if (haveHot && (!have || compare_island(hot, match) > 0)) {
             match = hot;
             have = true;
+            source = 2;
         }
     }
+    if (detail) detail->finalSource = source;
     if (!have) {
         Island none{};
         none.radiusUsed = radius;
@@ -555,11 +573,12 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     // Exact stage: the regions are independent, so up to ectx.size() of them are
     // resolved at once, each by a host thread on its own stream and scratch.
     std::vector<Island> resolved(exactN);
+    std::vector<ResolveDetail> details(exactN);
     const int lanes = std::min<int>(static_cast<int>(h->ectx.size()), exactN);
     if (lanes <= 1) {
         for (int k = 0; k < exactN; ++k)
             resolved[k] = resolve(h, h->ectx[0], ex[k].world, center_chunk_x(ex[k].center),
-                                  center_chunk_z(ex[k].center), radius, info[k].coarse, ms);
+                                  center_chunk_z(ex[k].center), radius, info[k].coarse, ms, &details[k]);
     } else {
         std::atomic<int> next{0};
         std::vector<std::string> errors(lanes);
@@ -568,7 +587,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
                 check(cudaSetDevice(h->cfg.device), "cudaSetDevice");
                 for (int k = next.fetch_add(1); k < exactN; k = next.fetch_add(1))
                     resolved[k] = resolve(h, h->ectx[t], ex[k].world, center_chunk_x(ex[k].center),
-                                          center_chunk_z(ex[k].center), radius, info[k].coarse, ms);
+                                          center_chunk_z(ex[k].center), radius, info[k].coarse, ms, &details[k]);
             } catch (const std::exception& e) {
                 errors[t] = e.what();
                 next.store(exactN);
@@ -603,6 +622,12 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
             r.coarse = info[k].coarse;
             r.p19_score = info[k].p19Score;
             to_island(isl, &r.island);
+            to_island(details[k].raw, &r.raw_island);
+            to_island(details[k].hot, &r.hot_island);
+            r.hot_scanned = details[k].hotScanned ? 1 : 0;
+            r.final_source = details[k].finalSource;
+            r.p19_pass = info[k].p19Pass;
+            r.p19_extreme = info[k].p19Extreme;
         }
     }
     h->stageMs[3] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - exactStart).count();

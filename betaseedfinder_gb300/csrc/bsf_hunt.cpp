@@ -1,0 +1,279 @@
+// Headless MEGA hunt for bsf_worker: the reference app's GPU search loop
+// (IslandSearchEngine.java:1314-1443, batches of worlds from deterministic
+// seeds, one attempt per region) and its candidate log, hunter_candidates.csv
+// (initializeCandidateCsv / appendCandidateCsv, IslandSearchEngine.java:4826-4960),
+// written from the C ABI's MEGA records, plus a run manifest.
+//
+//   bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.]
+//                   [capacity=32768] [min_blocks=1000]
+//   bsf_worker javafmt <value> <precision>      (formatting check: Java's %.<p>f)
+#include "../../include/bsf.h"
+
+#include <charconv>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace bsfhunt {
+
+// deterministicSeedForAttempt (IslandSearchEngine.java:2551-2556), SplitMix64.
+std::int64_t seed_for_attempt(std::int64_t sequenceSeed, std::int64_t attempt) {
+    std::uint64_t z = static_cast<std::uint64_t>(sequenceSeed) +
+                      static_cast<std::uint64_t>(attempt) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return static_cast<std::int64_t>(z ^ (z >> 31));
+}
+
+// Java's String.format(Locale.US, "%.<prec>f", v): the shortest decimal digits
+// that identify v, rounded half-up at <prec> fractional places.
+std::string java_fixed(double v, int prec) {
+    if (std::isnan(v)) return "NaN";
+    if (std::isinf(v)) return v > 0 ? "Infinity" : "-Infinity";
+    char buf[64];
+    const auto res = std::to_chars(buf, buf + sizeof(buf), v, std::chars_format::scientific);
+    std::string sci(buf, res.ptr);
+    bool neg = false;
+    if (!sci.empty() && sci[0] == '-') {
+        neg = true;
+        sci.erase(0, 1);
+    }
+    const std::size_t ePos = sci.find('e');
+    std::string digits;
+    for (std::size_t i = 0; i < ePos; ++i)
+        if (sci[i] != '.') digits.push_back(sci[i]);
+    const int exp10 = std::atoi(sci.c_str() + ePos + 1);  // value = d.ddd x 10^exp10
+    // integer part digits = exp10 + 1; place the digits on a fixed grid
+    int intLen = exp10 + 1;
+    std::string intPart, frac;
+    if (intLen <= 0) {
+        intPart = "0";
+        frac = std::string(static_cast<std::size_t>(-intLen), '0') + digits;
+    } else if (static_cast<std::size_t>(intLen) >= digits.size()) {
+        intPart = digits + std::string(static_cast<std::size_t>(intLen) - digits.size(), '0');
+    } else {
+        intPart = digits.substr(0, static_cast<std::size_t>(intLen));
+        frac = digits.substr(static_cast<std::size_t>(intLen));
+    }
+    bool roundUp = false;
+    if (frac.size() > static_cast<std::size_t>(prec)) {
+        roundUp = frac[static_cast<std::size_t>(prec)] >= '5';
+        frac.resize(static_cast<std::size_t>(prec));
+    }
+    frac.resize(static_cast<std::size_t>(prec), '0');
+    if (roundUp) {
+        std::string all = intPart + frac;
+        int i = static_cast<int>(all.size()) - 1;
+        for (; i >= 0; --i) {
+            if (all[static_cast<std::size_t>(i)] == '9') {
+                all[static_cast<std::size_t>(i)] = '0';
+            } else {
+                ++all[static_cast<std::size_t>(i)];
+                break;
+            }
+        }
+        if (i < 0) all.insert(all.begin(), '1');
+        intPart = all.substr(0, all.size() - static_cast<std::size_t>(prec));
+        frac = all.substr(all.size() - static_cast<std::size_t>(prec));
+    }
+    std::string out = neg ? "-" : "";
+    out += intPart;
+    if (prec > 0) out += "." + frac;
+    return out;
+}
+
+const char* jbool(bool b) { return b ? "true" : "false"; }
+
+const char* kHeader =
+    "attempt,seed,stage0,stage0Y88,coarse,p20,upper,high,p19Pass,p19Score,p19Extreme,searchCenterChunkX,"
+    "searchCenterChunkZ,matched,status,rawBlocks,verifiedBlocks,rawRadius,verifiedRadius,rawTouchesSide,"
+    "verifiedTouchesSide,columns,width,depth,footprintArea,fillPercent,avgThickness,minY,maxY,centerX,centerZ,"
+    "minX,maxX,minZ,maxZ,hotScanned,hotRadius,hotBlocks,hotTouchesSide,finalSource\n";
+
+// One candidate line (appendCandidateCsv): raw = the scan at the search radius
+// after border verification, verified = the chosen island, hot = the hot scan.
+std::string candidate_line(std::int64_t attempt, const bsf_mega_record& r, bool duplicate) {
+    const bsf_island& raw = r.raw_island;
+    const bsf_island& fin = r.island;
+    const bsf_island& hot = r.hot_island;
+    const bool haveRaw = raw.found != 0, haveFinal = fin.found != 0, haveHot = hot.found != 0;
+    const bool finalIsHot = haveFinal && r.final_source == 2;
+    const bool matched = haveFinal && !duplicate;
+    // the final island is the raw scan's or the hot scan's: never a border-verified replacement
+    const char* finalSource = duplicate ? "duplicate_merged" : (finalIsHot ? "hot_scan" : (haveFinal ? "raw" : "none"));
+    const char* status;
+    if (duplicate) status = "duplicate_region_merged";
+    else if (haveFinal && finalIsHot && fin.touches_side) status = "matched_hot_scan_still_touches_side";
+    else if (haveFinal && finalIsHot) status = "matched_hot_scan";
+    else if (haveFinal && fin.touches_side) status = "matched_still_touches_side";
+    else if (haveFinal) status = "matched";
+    else if (haveRaw) status = "border_rejected_or_invalid";
+    else if (r.hot_scanned) status = "hot_scan_no_match";
+    else status = "no_match";
+    // finalComponent = verified if any, else raw
+    const bsf_island& comp = haveFinal ? fin : raw;
+    const bool haveComp = haveFinal || haveRaw;
+    const int columns = haveComp ? comp.columns : 0;
+    const int width = haveComp ? comp.max_x - comp.min_x + 1 : 0;
+    const int depth = haveComp ? comp.max_z - comp.min_z + 1 : 0;
+    const int area = width * depth;
+    const double fill = haveComp ? 100.0 * comp.columns / static_cast<double>(area > 1 ? area : 1) : 0.0;
+    const double thick = haveComp ? comp.blocks / static_cast<double>(comp.columns > 1 ? comp.columns : 1) : 0.0;
+    char buf[1024];
+    std::snprintf(buf, sizeof(buf),
+                  "%lld,%lld,%d,%d,%d,%d,%d,%d,%s,%s,%s,%d,%d,%s,%s,%d,%d,%d,%d,%s,%s,%d,%d,%d,%d,%s,%s,%d,%d,%d,%d,%d,"
+                  "%d,%d,%d,%s,%d,%d,%s,%s\n",
+                  static_cast<long long>(attempt), static_cast<long long>(r.seed), r.high, r.high, r.coarse, r.p20,
+                  r.upper, r.high, jbool(r.p19_pass != 0), java_fixed(r.p19_score, 6).c_str(),
+                  jbool(r.p19_extreme != 0), r.center_chunk_x, r.center_chunk_z, jbool(matched), status,
+                  haveRaw ? raw.blocks : 0, haveFinal ? fin.blocks : 0, haveRaw ? raw.radius_used : 0,
+                  haveFinal ? fin.radius_used : 0, jbool(haveRaw && raw.touches_side),
+                  jbool(haveFinal && fin.touches_side), columns, width, depth, area, java_fixed(fill, 4).c_str(),
+                  java_fixed(thick, 4).c_str(), haveComp ? comp.min_y : 0, haveComp ? comp.max_y : 0,
+                  haveComp ? comp.center_x : 0, haveComp ? comp.center_z : 0, haveComp ? comp.min_x : 0,
+                  haveComp ? comp.max_x : 0, haveComp ? comp.min_z : 0, haveComp ? comp.max_z : 0,
+                  jbool(r.hot_scanned != 0), haveHot ? hot.radius_used : 0, haveHot ? hot.blocks : 0,
+                  jbool(haveHot && hot.touches_side), finalSource);
+    return buf;
+}
+
+int parse_profile_name(const std::string& v) {
+    if (v == "general") return BSF_PROFILE_GENERAL;
+    if (v == "mega") return BSF_PROFILE_MEGA;
+    if (v == "record60") return BSF_PROFILE_RECORD60;
+    if (v == "record80") return BSF_PROFILE_RECORD80;
+    throw std::invalid_argument("unknown profile " + v);
+}
+
+int hunt_main(int argc, char** argv) {
+    if (argc < 4) throw std::invalid_argument("hunt needs <sequence_seed> <regions>");
+    const std::int64_t sequenceSeed = std::strtoll(argv[2], nullptr, 10);
+    const std::int64_t regionsToCheck = std::strtoll(argv[3], nullptr, 10);
+    const std::string profileName = argc > 4 ? argv[4] : "mega";
+    const int profile = parse_profile_name(profileName);
+    const int radius = argc > 5 ? std::atoi(argv[5]) : 7;
+    const std::string outdir = argc > 6 ? argv[6] : ".";
+    const std::uint32_t capacity = argc > 7 ? static_cast<std::uint32_t>(std::strtoul(argv[7], nullptr, 10)) : 32768u;
+    const int minBlocks = argc > 8 ? std::atoi(argv[8]) : 1000;
+    if (regionsToCheck <= 0 || capacity == 0 || radius < 0 || radius > 24)
+        throw std::invalid_argument("hunt: regions and capacity must be positive and radius 0..24");
+
+    bsf_config cfg;
+    bsf_default_config(&cfg);
+    cfg.capacity = capacity;
+    cfg.profile = profile;
+    cfg.centers = 8;
+    cfg.max_exact_radius = 24;
+    void* h = bsf_open(&cfg);
+    if (!h) throw std::runtime_error("bsf_open failed");
+    if (bsf_last_error(h)[0]) {
+        const std::string e = bsf_last_error(h);
+        bsf_close(h);
+        throw std::runtime_error("bsf_open: " + e);
+    }
+    bsf_match_settings ms;
+    bsf_default_match_settings(&ms);
+    ms.min_blocks = minBlocks;
+
+    const std::string csvPath = outdir + "/hunter_candidates.csv";
+    std::FILE* csv = std::fopen(csvPath.c_str(), "wb");
+    if (!csv) {
+        bsf_close(h);
+        throw std::runtime_error("cannot write " + csvPath);
+    }
+    std::fputs(kHeader, csv);
+
+    const int centers = 8;
+    std::vector<std::int64_t> seeds(capacity);
+    std::vector<bsf_mega_record> recs(capacity * static_cast<std::size_t>(centers));
+    std::set<std::tuple<std::int64_t, int, int, int, int, int, int, int, int>> seen;  // registerUniqueMatch keys
+    std::int64_t issuedRegions = 0, issuedWorlds = 0, candidates = 0, matches = 0, duplicates = 0, bestBlocks = 0;
+    bsf_stage_counts total{};
+    const auto t0 = std::chrono::steady_clock::now();
+    while (issuedRegions < regionsToCheck) {
+        const std::int64_t remaining = regionsToCheck - issuedRegions;
+        const int regionsThisBatch = static_cast<int>(std::min<std::int64_t>(
+            static_cast<std::int64_t>(capacity) * centers, remaining));
+        const int count = (regionsThisBatch + centers - 1) / centers;
+        for (int i = 0; i < count; ++i) seeds[i] = seed_for_attempt(sequenceSeed, issuedWorlds + i + 1);
+        std::uint32_t n = 0;
+        bsf_stage_counts c{};
+        const int rc = bsf_mega_search(h, seeds.data(), static_cast<std::uint32_t>(count), radius, &ms, recs.data(),
+                                       static_cast<std::uint32_t>(recs.size()), &n, &c);
+        if (rc != BSF_OK) {
+            const std::string e = bsf_last_error(h);
+            std::fclose(csv);
+            bsf_close(h);
+            throw std::runtime_error("bsf_mega_search: " + e);
+        }
+        for (std::size_t f = 0; f < sizeof(bsf_stage_counts) / sizeof(uint64_t); ++f)
+            reinterpret_cast<uint64_t*>(&total)[f] += reinterpret_cast<const uint64_t*>(&c)[f];
+        for (std::uint32_t k = 0; k < n; ++k) {
+            const bsf_mega_record& r = recs[k];
+            const int regionOffset = r.world_index * centers + r.center_index;
+            if (regionOffset >= regionsThisBatch) continue;  // centres past the requested region count
+            bool duplicate = false;
+            if (r.island.found) {
+                const auto key = std::make_tuple(r.seed, r.island.min_x, r.island.max_x, r.island.min_z,
+                                                 r.island.max_z, r.island.min_y, r.island.max_y, r.island.blocks,
+                                                 r.island.columns);
+                duplicate = !seen.insert(key).second;
+                if (duplicate) ++duplicates;
+                else {
+                    ++matches;
+                    if (r.island.blocks > bestBlocks) bestBlocks = r.island.blocks;
+                }
+            }
+            const std::int64_t attempt = issuedRegions + regionOffset + 1;
+            std::fputs(candidate_line(attempt, r, duplicate).c_str(), csv);
+            ++candidates;
+        }
+        issuedWorlds += count;
+        issuedRegions += regionsThisBatch;
+    }
+    std::fclose(csv);
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    bsf_close(h);
+
+    const std::string manifestPath = outdir + "/run_manifest.json";
+    std::FILE* m = std::fopen(manifestPath.c_str(), "wb");
+    if (!m) throw std::runtime_error("cannot write " + manifestPath);
+    std::fprintf(m,
+                 "{\n  \"mode\": \"gpu_hunt\",\n  \"deterministicSeedSequenceSeed\": %lld,\n  \"seedsToCheck\": %lld,\n"
+                 "  \"worldsChecked\": %lld,\n  \"profile\": \"%s\",\n  \"chunkRadius\": %d,\n  \"minBlocks\": %d,\n"
+                 "  \"candidates\": %lld,\n  \"matches\": %lld,\n  \"duplicateRegionHits\": %lld,\n"
+                 "  \"bestBlocks\": %lld,\n  \"p20Passed\": %llu,\n  \"upperPassed\": %llu,\n  \"highPassed\": %llu,\n"
+                 "  \"p19Passed\": %llu,\n  \"megaRejected\": %llu,\n  \"coarseEvaluated\": %llu,\n"
+                 "  \"coarsePassed\": %llu,\n  \"elapsedSeconds\": %.3f\n}\n",
+                 static_cast<long long>(sequenceSeed), static_cast<long long>(regionsToCheck),
+                 static_cast<long long>(issuedWorlds), profileName.c_str(), radius, minBlocks,
+                 static_cast<long long>(candidates), static_cast<long long>(matches),
+                 static_cast<long long>(duplicates), static_cast<long long>(bestBlocks),
+                 static_cast<unsigned long long>(total.p20_passed), static_cast<unsigned long long>(total.upper_passed),
+                 static_cast<unsigned long long>(total.high_passed), static_cast<unsigned long long>(total.p19_passed),
+                 static_cast<unsigned long long>(total.mega_rejected),
+                 static_cast<unsigned long long>(total.coarse_evaluated),
+                 static_cast<unsigned long long>(total.coarse_passed), secs);
+    std::fclose(m);
+    std::fprintf(stderr, "HUNT DONE | regions=%lld worlds=%lld candidates=%lld matches=%lld duplicates=%lld | %.2f s\n",
+                 static_cast<long long>(regionsToCheck), static_cast<long long>(issuedWorlds),
+                 static_cast<long long>(candidates), static_cast<long long>(matches),
+                 static_cast<long long>(duplicates), secs);
+    return 0;
+}
+
+int javafmt_main(int argc, char** argv) {
+    if (argc < 4) throw std::invalid_argument("javafmt needs <value> <precision>");
+    std::printf("%s\n", java_fixed(std::strtod(argv[2], nullptr), std::atoi(argv[3])).c_str());
+    return 0;
+}
+
+}  // namespace bsfhunt

@@ -3,6 +3,8 @@
 //   bsf_worker stage0stream [capacity=32768] [general|mega|record60|record80] [research|lean] [centers=1|8]
 //   bsf_worker stream [capacity=32768]
 //   bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]
+//   bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.] [capacity=32768]
+//                   [min_blocks=1000]      (headless search writing hunter_candidates.csv, bsf_hunt.cpp)
 //
 // stage0stream / stream keep the reference protocol byte for byte
 // (gpu_p20_benchmark.cpp:7310-7685; Java side src/GpuStage0Scout.java:143-335,
@@ -222,6 +224,11 @@ int megastream(std::uint32_t capacity, int profile, int radius) {
 
 }  // namespace
 
+namespace bsfhunt {
+int hunt_main(int argc, char** argv);
+int javafmt_main(int argc, char** argv);
+}  // namespace bsfhunt
+
 int main(int argc, char** argv) {
     try {
         if (argc < 2) {
@@ -230,10 +237,14 @@ int main(int argc, char** argv) {
                          "  bsf_worker stage0stream [capacity=32768] [general|mega|record60|record80] [research|lean] "
                          "[centers=1|8]\n"
                          "  bsf_worker stream [capacity=32768]\n"
-                         "  bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]\n");
+                         "  bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]\n"
+                         "  bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.] "
+                         "[capacity=32768] [min_blocks=1000]\n");
             return 1;
         }
         const std::string mode = argv[1];
+        if (mode == "hunt") return bsfhunt::hunt_main(argc, argv);
+        if (mode == "javafmt") return bsfhunt::javafmt_main(argc, argv);
         const std::uint32_t cap = argc > 2 ? static_cast<std::uint32_t>(std::strtoul(argv[2], nullptr, 10)) : 32768u;
         if (mode == "stream") return p20stream(cap);
         if (mode == "stage0stream") {

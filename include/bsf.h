@@ -69,7 +69,14 @@ typedef struct bsf_mega_record {
     int32_t center_chunk_x, center_chunk_z;
     int32_t p20, upper, high, coarse;
     double p19_score;
-    bsf_island island;      /* found == 0 when no island matched */
+    bsf_island island;      /* the chosen island (found == 0 when no island matched) */
+    /* How it was chosen (processGpuRegionAttempt, src/IslandSearchEngine.java:1878-1971),
+     * for the candidate log (hunter_candidates.csv): */
+    bsf_island raw_island;  /* the scan at `radius` after side-border verification (found == 0: none) */
+    bsf_island hot_island;  /* the radius-16 hot scan after verification (found == 0: none or not run) */
+    int32_t hot_scanned;    /* 1 when the hot scan ran (coarse >= 120 and radius < 16) */
+    int32_t final_source;   /* 0 no island, 1 the raw scan, 2 the hot scan */
+    int32_t p19_pass, p19_extreme;
 } bsf_mega_record;
 
 typedef struct bsf_stage_counts {

@@ -111,3 +111,14 @@ def test_server_config_validation_without_a_gpu(lib):
     r = bsf.ServerResult()
     assert lib.bsf_server_poll(s, 1, 0, ctypes.byref(r)) == -1  # unknown ticket
     lib.bsf_server_close(s)
+
+
+@pytest.mark.parametrize("value,prec,expected", [
+    ("1.03125", 4, "1.0313"), ("2.675", 2, "2.68"), ("12.5", 4, "12.5000"), ("0.5", 0, "1"),
+    ("-1.25", 1, "-1.3"), ("99.99995", 4, "100.0000"), ("nan", 6, "NaN"), ("0.000123456", 6, "0.000123"),
+])
+def test_candidate_log_formats_numbers_like_java(lib, value, prec, expected):
+    """hunter_candidates.csv numbers follow Java's String.format("%.nf"): the
+    shortest decimal digits of the double, rounded half-up (2.675 -> 2.68)."""
+    out = subprocess.run([bsf.WORKER_PATH, "javafmt", value, str(prec)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == expected

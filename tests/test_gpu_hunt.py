@@ -1,0 +1,53 @@
+"""Headless hunt (bsf_worker hunt): the candidate log has the reference's
+header and one row per exact-stage region, each row agreeing with the MEGA
+record of the same region through the C ABI."""
+import csv
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import betaseedfinder_gb300 as bsf
+
+pytestmark = pytest.mark.gpu
+
+HEADER = ("attempt,seed,stage0,stage0Y88,coarse,p20,upper,high,p19Pass,p19Score,p19Extreme,searchCenterChunkX,"
+          "searchCenterChunkZ,matched,status,rawBlocks,verifiedBlocks,rawRadius,verifiedRadius,rawTouchesSide,"
+          "verifiedTouchesSide,columns,width,depth,footprintArea,fillPercent,avgThickness,minY,maxY,centerX,centerZ,"
+          "minX,maxX,minZ,maxZ,hotScanned,hotRadius,hotBlocks,hotTouchesSide,finalSource")
+
+
+def test_hunt_writes_reference_candidate_rows(tmp_path):
+    seq, worlds = 7_123_456_789, 16000
+    regions = 8 * worlds - 3                        # the last world has 5 of its 8 centres
+    # two batches of 8192 worlds: attempts continue across batches
+    out = subprocess.run([bsf.WORKER_PATH, "hunt", str(seq), str(regions), "mega", "7", str(tmp_path), "8192"],
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    text = open(os.path.join(tmp_path, "hunter_candidates.csv")).read()
+    assert text.splitlines()[0] == HEADER
+    rows = list(csv.DictReader(text.splitlines()))
+    seeds = np.array([bsf.splitmix_seed(seq, a) for a in range(1, worlds + 1)], dtype=np.int64)
+    with bsf.Worker(capacity=worlds, profile="mega", centers=8, max_exact_radius=24) as w:
+        _, recs = w.mega_search(seeds, radius=7)
+    recs = [r for r in recs if r.world_index * 8 + r.center_index < regions]
+    assert len(rows) == len(recs) > 0
+    for row, r in zip(rows, recs):
+        assert int(row["attempt"]) == r.world_index * 8 + r.center_index + 1
+        assert int(row["seed"]) == r.seed
+        assert (int(row["coarse"]), int(row["p20"]), int(row["upper"]), int(row["high"])) == \
+               (r.coarse, r.p20, r.upper, r.high)
+        assert int(row["stage0"]) == int(row["stage0Y88"]) == r.high
+        assert row["p19Pass"] == "true"
+        assert (int(row["searchCenterChunkX"]), int(row["searchCenterChunkZ"])) == (r.center_chunk_x, r.center_chunk_z)
+        assert row["matched"] == ("true" if r.island.found else "false")
+        if r.island.found:
+            assert int(row["verifiedBlocks"]) == r.island.blocks and int(row["columns"]) == r.island.columns
+            assert int(row["width"]) == r.island.max_x - r.island.min_x + 1
+            assert row["status"].startswith("matched") or row["status"] == "duplicate_region_merged"
+            assert row["finalSource"] in ("raw", "hot_scan", "duplicate_merged")
+        else:
+            assert row["status"] in ("no_match", "hot_scan_no_match") and row["finalSource"] == "none"
+    manifest = open(os.path.join(tmp_path, "run_manifest.json")).read()
+    assert '"seedsToCheck": %d' % regions in manifest and '"worldsChecked": %d' % worlds in manifest
