@@ -111,7 +111,7 @@ EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
-           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
+           "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_last_region_records", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
            "bsf_server_records", "bsf_server_preview_columns", "bsf_server_release", "bsf_server_get_stats"]
 
@@ -171,6 +171,7 @@ def load(path=LIB_PATH):
     L.bsf_server_submit_range.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, P(MatchSettings),
                                           u64p]
     L.bsf_set_profile.argtypes = [vp, ctypes.c_int32]
+    L.bsf_last_region_records.argtypes = [vp, u8p, ctypes.c_size_t]
     L.bsf_server_submit_preview.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                             P(MatchSettings), u64p]
     L.bsf_server_poll.argtypes = [vp, ctypes.c_uint64, ctypes.c_int32, P(ServerResult)]
@@ -280,6 +281,12 @@ class Worker:
     def footprint(self):
         """Device bytes this handle holds."""
         return int(load().bsf_handle_footprint(self._h))
+
+    def last_region_records(self, worlds):
+        """34-byte research records of every region of the last MEGA batch (`worlds` worlds)."""
+        out = np.zeros(worlds * self.cfg.centers * 34, np.uint8)
+        self._check(load().bsf_last_region_records(self._h, _p(out, ctypes.c_uint8), out.nbytes))
+        return out
 
     def set_profile(self, profile):
         self._check(load().bsf_set_profile(self._h, PROFILES.get(profile, profile) if isinstance(profile, str)

@@ -158,6 +158,7 @@ struct BsfHandle {
     std::vector<ExactCtx> ectx;  // exact-scan contexts (0: the handle's own)
     int capacity = 0;
     int centers = 8;
+    int lastBatch = 0;  // worlds in the last MEGA batch (their RegionInfo stays in dRegions)
     int coarseCap = 0;
     int exactCap = 0;
 
@@ -631,6 +632,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
         }
     }
     h->stageMs[3] = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - exactStart).count();
+    h->lastBatch = n;
     if (recordsCount) *recordsCount = written;
     if (counts) {
         counts->worlds = count;
@@ -832,6 +834,23 @@ int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
 uint64_t bsf_handle_footprint(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     return h ? h->footprint : 0;
+}
+
+int bsf_last_region_records(void* hv, uint8_t* out, size_t outLen) {
+    return guarded(hv, [&](BsfHandle* h) {
+        const int regions = h->lastBatch * h->centers;
+        const std::size_t need = static_cast<std::size_t>(regions) * 34;
+        if (!out || outLen < need || regions == 0)
+            throw std::invalid_argument("bsf_last_region_records: no MEGA batch yet, or out_len too small");
+        // dOut holds max(records, capacity * 4096) bytes: 34-byte records of every region always fit
+        if (need > std::max<std::size_t>(h->outBytes, static_cast<std::size_t>(h->capacity) * 4096))
+            throw std::length_error("bsf_last_region_records: output staging too small");
+        k_pack_records<<<(regions + 255) / 256, 256, 0, h->stream>>>(h->dRegions, regions, 1, h->dOut);
+        ++h->launches;
+        check(cudaGetLastError(), "k_pack_records");
+        d2h(h, out, h->dOut, need, "region records");
+        return BSF_OK;
+    });
 }
 
 int bsf_set_profile(void* hv, int32_t profile) {

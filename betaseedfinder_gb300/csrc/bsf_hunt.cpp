@@ -2,10 +2,13 @@
 // (IslandSearchEngine.java:1314-1443, batches of worlds from deterministic
 // seeds, one attempt per region) and its candidate log, hunter_candidates.csv
 // (initializeCandidateCsv / appendCandidateCsv, IslandSearchEngine.java:4826-4960),
-// written from the C ABI's MEGA records, plus a run manifest.
+// written from the C ABI's MEGA records, plus a run manifest. With an audit mask
+// it also re-scans a sample of rejected regions exactly and logs them like the
+// reference's record_reject_audits.csv (processLeanRejectAudit,
+// IslandSearchEngine.java:2126-2188; sampling :1403-1476, 2512-2529).
 //
 //   bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.]
-//                   [capacity=32768] [min_blocks=1000]
+//                   [capacity=32768] [min_blocks=1000] [audit_mask=0]
 //   bsf_worker javafmt <value> <precision>      (formatting check: Java's %.<p>f)
 #include "../../include/bsf.h"
 
@@ -145,6 +148,37 @@ std::string candidate_line(std::int64_t attempt, const bsf_mega_record& r, bool 
     return buf;
 }
 
+const char* kAuditHeader =
+    "attempt,seed,searchCenterChunkX,searchCenterChunkZ,rejectStage,rejectReason,p20,upper,high,p19Pass,p19Score,"
+    "p19Extreme,coarse,exactScanMs,exactMatched,exactBlocks,exactColumns,exactWidth,exactDepth,exactMinY,exactMaxY,"
+    "exactRadiusUsed,exactTouchesSideBorder\n";
+
+// The worker profile's gates (HuntProfileConfig, gpu_p20_benchmark.cpp:7262-7290).
+struct Gates {
+    int p20, upper, high, coarse;
+};
+Gates gates_of(int profile) {
+    switch (profile) {
+        case BSF_PROFILE_MEGA: return Gates{1, 8, 6, 85};
+        case BSF_PROFILE_RECORD60: return Gates{3, 19, 12, 95};
+        case BSF_PROFILE_RECORD80: return Gates{3, 19, 20, 700};
+        default: return Gates{1, 5, 5, 85};
+    }
+}
+
+const char* reject_name(int stage) {  // rejectStageName (IslandSearchEngine.java:2190-2201)
+    switch (stage) {
+        case 1: return "p20";
+        case 2: return "upper";
+        case 3: return "reentry";
+        case 4: return "high";
+        case 5: return "p19";
+        case 6: return "coarse";
+        case 7: return "mega_topology";
+        default: return "unknown";
+    }
+}
+
 int parse_profile_name(const std::string& v) {
     if (v == "general") return BSF_PROFILE_GENERAL;
     if (v == "mega") return BSF_PROFILE_MEGA;
@@ -163,6 +197,12 @@ int hunt_main(int argc, char** argv) {
     const std::string outdir = argc > 6 ? argv[6] : ".";
     const std::uint32_t capacity = argc > 7 ? static_cast<std::uint32_t>(std::strtoul(argv[7], nullptr, 10)) : 32768u;
     const int minBlocks = argc > 8 ? std::atoi(argv[8]) : 1000;
+    // audits: rejected regions with (seed & mask) == 0, P20 rejects with (attempt & p20Mask) == 0
+    // (the record profiles use the same mask; the others 32767, IslandSearchEngine.java:2520-2525)
+    const std::int64_t auditMask = argc > 9 ? std::strtoll(argv[9], nullptr, 10) : 0;
+    const std::int64_t p20AuditMask =
+        (profile == BSF_PROFILE_RECORD60 || profile == BSF_PROFILE_RECORD80) ? auditMask : 32767;
+    const Gates gate = gates_of(profile);
     if (regionsToCheck <= 0 || capacity == 0 || radius < 0 || radius > 24)
         throw std::invalid_argument("hunt: regions and capacity must be positive and radius 0..24");
 
@@ -190,6 +230,18 @@ int hunt_main(int argc, char** argv) {
         throw std::runtime_error("cannot write " + csvPath);
     }
     std::fputs(kHeader, csv);
+    std::FILE* audits = nullptr;
+    if (auditMask > 0) {
+        audits = std::fopen((outdir + "/record_reject_audits.csv").c_str(), "wb");
+        if (!audits) {
+            std::fclose(csv);
+            bsf_close(h);
+            throw std::runtime_error("cannot write record_reject_audits.csv");
+        }
+        std::fputs(kAuditHeader, audits);
+    }
+    std::vector<std::uint8_t> regionRecs(audits ? capacity * static_cast<std::size_t>(8) * 34 : 0);
+    std::int64_t audited = 0, auditHits = 0;
 
     const int centers = 8;
     std::vector<std::int64_t> seeds(capacity);
@@ -236,10 +288,67 @@ int hunt_main(int argc, char** argv) {
             std::fputs(candidate_line(attempt, r, duplicate).c_str(), csv);
             ++candidates;
         }
+        if (audits) {
+            if (bsf_last_region_records(h, regionRecs.data(), regionRecs.size()) != BSF_OK) {
+                const std::string e = bsf_last_error(h);
+                std::fclose(csv);
+                std::fclose(audits);
+                bsf_close(h);
+                throw std::runtime_error("bsf_last_region_records: " + e);
+            }
+            for (int ro = 0; ro < regionsThisBatch; ++ro) {
+                const std::uint8_t* q = regionRecs.data() + static_cast<std::size_t>(ro) * 34;
+                const int p20 = q[0], upper = q[1], high = q[2];
+                const bool p19Pass = q[3] != 0, extreme = q[6] != 0, mega = q[7] != 0;
+                const int coarse = q[4] | (q[5] << 8);
+                double p19Score;
+                std::memcpy(&p19Score, q + 8, 8);
+                int stage;  // rejectStage (IslandSearchEngine.java:1368-1376), with the worker's gates
+                if (p20 < gate.p20) stage = 1;
+                else if (upper < gate.upper) stage = 2;
+                else if (high < gate.high) stage = 4;
+                else if (!p19Pass) stage = 5;
+                else if (mega) stage = 7;
+                else if (coarse < gate.coarse) stage = 6;
+                else stage = 0;
+                const std::int64_t attempt = issuedRegions + ro + 1;
+                const std::int64_t seed = seeds[ro / centers];
+                const bool sampled = stage == 1 ? (attempt & p20AuditMask) == 0
+                                                : (stage != 0 && stage != 7 && (seed & auditMask) == 0);
+                if (!sampled) continue;
+                // GpuStage0Scout centres (src/GpuStage0Scout.java:19-21)
+                static const int kCx[8] = {0, 15, 0, 15, -15, -15, 0, 15};
+                static const int kCz[8] = {0, 0, 15, 15, 0, 15, -15, -15};
+                const int cx = kCx[ro % centers], cz = kCz[ro % centers];
+                bsf_island isl{};
+                const auto a0 = std::chrono::steady_clock::now();
+                if (bsf_exact_scan(h, seed, cx, cz, radius, &ms, &isl) != BSF_OK) {
+                    const std::string e = bsf_last_error(h);
+                    std::fclose(csv);
+                    std::fclose(audits);
+                    bsf_close(h);
+                    throw std::runtime_error("bsf_exact_scan: " + e);
+                }
+                const double ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a0).count();
+                char line[512];
+                std::snprintf(line, sizeof(line), "%lld,%lld,%d,%d,%d,%s,%d,%d,%d,%s,%s,%s,%d,%s,%s,%d,%d,%d,%d,%d,%d,%d,%s\n",
+                              static_cast<long long>(attempt), static_cast<long long>(seed), cx, cz, stage,
+                              reject_name(stage), p20, upper, high, jbool(p19Pass), java_fixed(p19Score, 6).c_str(),
+                              jbool(extreme), coarse, java_fixed(ms_, 3).c_str(), jbool(isl.found != 0),
+                              isl.found ? isl.blocks : 0, isl.found ? isl.columns : 0,
+                              isl.found ? isl.max_x - isl.min_x + 1 : 0, isl.found ? isl.max_z - isl.min_z + 1 : 0,
+                              isl.found ? isl.min_y : -1, isl.found ? isl.max_y : -1,
+                              isl.found ? isl.radius_used : radius, jbool(isl.found && isl.touches_side));
+                std::fputs(line, audits);
+                ++audited;
+                if (isl.found) ++auditHits;
+            }
+        }
         issuedWorlds += count;
         issuedRegions += regionsThisBatch;
     }
     std::fclose(csv);
+    if (audits) std::fclose(audits);
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     bsf_close(h);
 
@@ -252,7 +361,8 @@ int hunt_main(int argc, char** argv) {
                  "  \"candidates\": %lld,\n  \"matches\": %lld,\n  \"duplicateRegionHits\": %lld,\n"
                  "  \"bestBlocks\": %lld,\n  \"p20Passed\": %llu,\n  \"upperPassed\": %llu,\n  \"highPassed\": %llu,\n"
                  "  \"p19Passed\": %llu,\n  \"megaRejected\": %llu,\n  \"coarseEvaluated\": %llu,\n"
-                 "  \"coarsePassed\": %llu,\n  \"elapsedSeconds\": %.3f\n}\n",
+                 "  \"coarsePassed\": %llu,\n  \"rejectAudits\": %lld,\n  \"rejectAuditMatches\": %lld,\n"
+                 "  \"elapsedSeconds\": %.3f\n}\n",
                  static_cast<long long>(sequenceSeed), static_cast<long long>(regionsToCheck),
                  static_cast<long long>(issuedWorlds), profileName.c_str(), radius, minBlocks,
                  static_cast<long long>(candidates), static_cast<long long>(matches),
@@ -261,7 +371,8 @@ int hunt_main(int argc, char** argv) {
                  static_cast<unsigned long long>(total.high_passed), static_cast<unsigned long long>(total.p19_passed),
                  static_cast<unsigned long long>(total.mega_rejected),
                  static_cast<unsigned long long>(total.coarse_evaluated),
-                 static_cast<unsigned long long>(total.coarse_passed), secs);
+                 static_cast<unsigned long long>(total.coarse_passed), static_cast<long long>(audited),
+                 static_cast<long long>(auditHits), secs);
     std::fclose(m);
     std::fprintf(stderr, "HUNT DONE | regions=%lld worlds=%lld candidates=%lld matches=%lld duplicates=%lld | %.2f s\n",
                  static_cast<long long>(regionsToCheck), static_cast<long long>(issuedWorlds),

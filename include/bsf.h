@@ -147,6 +147,11 @@ int bsf_mega_search_device(void* h, const int64_t* d_seeds, uint32_t count, int3
                            const bsf_match_settings* s, bsf_mega_record* records, uint32_t records_cap,
                            uint32_t* records_count, bsf_stage_counts* counts, void* stream);
 
+/* Stage outcomes of every region of the last bsf_mega_search(_device) batch:
+ * count * centers 34-byte research records (the stage0stream research layout,
+ * world-major, centre-minor), e.g. to sample rejected regions for exact audits. */
+int bsf_last_region_records(void* h, uint8_t* out, size_t out_len);
+
 /* Number of GPU kernel launches issued by the handle so far (instrumentation). */
 uint64_t bsf_kernel_launches(const void* h);
 

@@ -51,3 +51,33 @@ def test_hunt_writes_reference_candidate_rows(tmp_path):
             assert row["status"] in ("no_match", "hot_scan_no_match") and row["finalSource"] == "none"
     manifest = open(os.path.join(tmp_path, "run_manifest.json")).read()
     assert '"seedsToCheck": %d' % regions in manifest and '"worldsChecked": %d' % worlds in manifest
+
+
+def test_hunt_reject_audits_match_exact_scans(tmp_path):
+    """Audited rejects (seed & mask == 0) get an exact scan; each audit row
+    carries the region's stage outcome and the exact scan's island."""
+    seq, worlds, mask = 99_001, 3000, 15
+    out = subprocess.run([bsf.WORKER_PATH, "hunt", str(seq), str(8 * worlds), "mega", "5", str(tmp_path), "4096",
+                          "1000", str(mask)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    text = open(os.path.join(tmp_path, "record_reject_audits.csv")).read()
+    assert text.splitlines()[0] == (
+        "attempt,seed,searchCenterChunkX,searchCenterChunkZ,rejectStage,rejectReason,p20,upper,high,p19Pass,"
+        "p19Score,p19Extreme,coarse,exactScanMs,exactMatched,exactBlocks,exactColumns,exactWidth,exactDepth,"
+        "exactMinY,exactMaxY,exactRadiusUsed,exactTouchesSideBorder")
+    rows = list(csv.DictReader(text.splitlines()))
+    assert len(rows) > 20
+    seeds = np.array([bsf.splitmix_seed(seq, a) for a in range(1, worlds + 1)], dtype=np.int64)
+    with bsf.Worker(capacity=worlds, profile="mega", centers=8, max_exact_radius=24) as w:
+        w.mega_search(seeds, radius=5)
+        regs = bsf.decode_records(w.last_region_records(worlds), 34)
+        for row in rows[:40]:
+            region = int(row["attempt"]) - 1
+            seed = int(row["seed"])
+            assert seed == seeds[region // 8] and seed & mask == 0
+            assert int(row["p20"]) == regs["p20Counts"][region] and int(row["coarse"]) == regs["coarseScores"][region]
+            assert int(row["rejectStage"]) in (1, 2, 4, 5, 6)
+            isl = w.exact_scan(seed, int(row["searchCenterChunkX"]), int(row["searchCenterChunkZ"]), 5)
+            assert row["exactMatched"] == ("true" if isl.found else "false")
+            if isl.found:
+                assert int(row["exactBlocks"]) == isl.blocks and int(row["exactMinY"]) == isl.min_y
