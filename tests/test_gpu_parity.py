@@ -112,3 +112,20 @@ def test_resolve_region_with_hot_scan_matches_oracle(worker):
     g = worker.resolve_region(seed, 0, 0, 7, 130)
     o = po.resolve_region(seed, 0, 0, 7, 130)
     assert g.key() == o.key()
+
+
+def test_rng_rejection_seeds_match_oracle(worker):
+    """Worlds whose generator setup hits nextInt's rejection loop take the GPU's
+    serial rebuild of the affected stream; their bitmaps and Stage0 records must
+    still equal the oracle's (whose states are pinned to the reference's)."""
+    import json
+    import os
+    rej = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "rng_rejection_seeds.json")))
+    seeds = np.array(rej["seeds"], dtype=np.int64)
+    bm, h = worker.chunk_bitmaps(seeds, 0, 0)
+    obm, oh = po.chunk_bitmaps(seeds, 0, 0)
+    assert np.array_equal(bm, obm) and np.array_equal(h, oh)
+    with bsf.Worker(capacity=64, profile="mega", research=True, centers=8, max_exact_radius=24) as w:
+        assert np.array_equal(w.stage0_filter(seeds), po.stage0_batch(seeds, centers=8, profile=1, research=True))
+        counts, _ = w.mega_search(seeds)
+    assert counts.rng_fallbacks >= len(seeds)   # every one of them took the fallback path

@@ -91,3 +91,20 @@ def test_oracle_against_live_reference_random():
         L.or_perlin_column17_test(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, 0, P(a, ctypes.c_double))
         R.ref_perlin3_full17(P(perm, ctypes.c_uint8), P(abc, ctypes.c_double), x, sy, z, P(b, ctypes.c_double))
         assert _bits(a) == _bits(b)
+
+
+REJECT = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "rng_rejection_seeds.json")))
+
+
+def test_rejection_seed_states_match_reference():
+    """Worlds whose setup hits nextInt's rejection loop: the oracle's 76 generator
+    states equal the reference Random/initPerlin's, recorded as hashes."""
+    import hashlib
+    assert len(REJECT["seeds"]) >= 8
+    for sd in REJECT["seeds"]:
+        h = hashlib.sha256()
+        for idx in range(76):
+            perm, abc = po.world_state(sd, idx)
+            h.update(np.asarray(perm, np.uint8).tobytes())
+            h.update(np.asarray(abc, np.float64).view(np.uint64).tobytes())
+        assert h.hexdigest() == REJECT["ref_states_sha256"][str(sd)], sd
