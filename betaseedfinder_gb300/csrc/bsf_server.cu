@@ -464,8 +464,13 @@ void bsf_server_close(void* sv) {
 }
 
 const char* bsf_server_last_error(const void* sv) {
-    const Server* S = static_cast<const Server*>(sv);
-    return S ? S->err.c_str() : "null server";
+    // Workers rewrite the message under the lock; each caller thread gets its own copy.
+    thread_local std::string copy;
+    Server* S = const_cast<Server*>(static_cast<const Server*>(sv));
+    if (!S) return "null server";
+    std::lock_guard<std::mutex> lk(S->mu);
+    copy = S->err;
+    return copy.c_str();
 }
 
 int bsf_server_submit_range(void* sv, const int64_t* seeds, uint32_t count, int32_t radius, int32_t profile,
