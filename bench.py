@@ -458,17 +458,39 @@ def main():
 
     extras = {}
     if dist.rank == 0 and not args.skip_extras:
-        # plain stage-by-stage form on the same workload (spec comparison)
+        # plain stage-by-stage FP64 form on the same workload (spec comparison), timed
+        # alone; then both forms' per-region records of those batches are compared byte for byte
         worker.set_mode(bsf.MODE_PLAIN)
         torch.cuda.synchronize()
         p0 = time.perf_counter()
+        plain_out = []
         for s in range(args.plain_steps):
-            worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+            c, r = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+            plain_out.append((c.as_dict(), [(x.world_index, x.center_index, x.island.key()) for x in r]))
         torch.cuda.synchronize()
         plain = B * args.plain_steps / (time.perf_counter() - p0)
+        plain_regions = []
+        for s in range(args.plain_steps):  # untimed: the records of the same batches again, kept
+            worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+            plain_regions.append(worker.last_region_records(B))
         worker.set_mode(bsf.MODE_QUEUED)
+        mismatched_regions = 0
+        mismatched_batches = 0
+        for s in range(args.plain_steps):
+            c, r = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+            q = worker.last_region_records(B).reshape(-1, 34)
+            mismatched_regions += int((q != plain_regions[s].reshape(-1, 34)).any(axis=1).sum())
+            dq = {k: v for k, v in c.as_dict().items() if k not in ("rng_fallbacks", "screened_tasks", "fallback_tasks")}
+            dp = {k: v for k, v in plain_out[s][0].items() if k not in ("rng_fallbacks", "screened_tasks", "fallback_tasks")}
+            if dq != dp or [(x.world_index, x.center_index, x.island.key()) for x in r] != plain_out[s][1]:
+                mismatched_batches += 1
         extras["forms"] = {"queued_worlds_per_s": value / dist.world, "plain_worlds_per_s": plain,
-                           "queued_over_plain": (value / dist.world) / plain}
+                           "queued_over_plain": (value / dist.world) / plain,
+                           "verified": {"worlds": B * args.plain_steps, "regions": B * 8 * args.plain_steps,
+                                        "mismatched_region_records": mismatched_regions,
+                                        "mismatched_batches": mismatched_batches,
+                                        "against": "the FP64 plain form on the same seeds (34-byte region "
+                                                   "records, stage counts, island records)"}}
         if args.served_ranges > 0:
             served = served_form(args, bsf, seed_start(args.seed, dist.rank, 4))
             extras["served"] = served
