@@ -108,10 +108,10 @@ __device__ unsigned exact_bits(const CoarseSmem& s, double X, double Z, double d
 __device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int cz, int r) {
     if (r == 0) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
     if (r == 1) return exactwarp::exact_column_warp<6, 6>(s, cx, cz);
-    return exactwarp::exact_column_warp<12, 5>(s, cx, cz);
+    return exactwarp::exact_column_warp<12, TOP_SOLID_LEVEL - 11>(s, cx, cz);  // level 16: air
 }
 
-// Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,17)) by one
+// Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,16), level 16 is air) by one
 // thread: only when the fallback list of a tile overflows.
 __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int cz, int r) {
     const GenTable t = gtab(s);
@@ -137,7 +137,7 @@ __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int c
     column_shape(temp, rain, n4, n5, d5, d7);
     if (r == 0) return exact_bits<0, 6>(s, X, Z, d5, d7);
     if (r == 1) return exact_bits<6, 6>(s, X, Z, d5, d7);
-    return exact_bits<12, 5>(s, X, Z, d5, d7);
+    return exact_bits<12, TOP_SOLID_LEVEL - 11>(s, X, Z, d5, d7);
 }
 
 // Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds; kx is the half-local row.
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
                 if (forceExact) ok = false;
                 else if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
                 else if (r == 1) ok = screened_range<6, 6>(s, kx, kz, s.shape[c], bits);
-                else ok = screened_range<12, 5>(s, kx, kz, s.shape[c], bits);
+                else ok = screened_range<12, TOP_SOLID_LEVEL - 11>(s, kx, kz, s.shape[c], bits);  // 16 is air
                 if (ok) {
                     if (bits) atomicOr(&s.mask[c], bits);
                 } else {

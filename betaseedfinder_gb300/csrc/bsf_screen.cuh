@@ -355,6 +355,13 @@ __device__ __forceinline__ unsigned noise_select_f(float n1) {
     return 3u;
 }
 
+// Level 16 of a 17-level column is air everywhere: the top fade of
+// BetaTerrain173.java:808-830 has d13 = (float)(16 - 13) / 3.0F = 1.0 there, so
+// the density is d8 * 0.0 + -10.0 * 1.0 = -10.0 for any finite d8 (d5 >= 0.5
+// keeps d9, and so d8, finite). The screened kernels therefore evaluate levels
+// up to 15 and leave bit 16 clear.
+constexpr int TOP_SOLID_LEVEL = 15;
+
 // Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1
 // when decided, 0 when the FP64 value could have either sign.
 __device__ __forceinline__ int density_sign_f(int y, Fe d5, Fe d7, float n1, float n2, float n3) {

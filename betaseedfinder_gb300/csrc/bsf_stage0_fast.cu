@@ -123,7 +123,7 @@ __device__ unsigned exact_bits(const WorldSmem& s, double X, double Z, double d5
     return bits;
 }
 
-// Exact column for Y range id r: 0 -> [11,17), 1 -> [0,6), 2 -> [6,11).
+// Exact column for Y range id r: 0 -> [11,16) (level 16 is air), 1 -> [0,6), 2 -> [6,11).
 __device__ __noinline__ unsigned exact_task(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
@@ -148,7 +148,7 @@ __device__ __noinline__ unsigned exact_task(const WorldSmem& s, int c, int col, 
     }
     n5 = acc;
     column_shape(temp, rain, n4, n5, d5, d7);
-    if (r == 0) return exact_bits<11, 6>(s, X, Z, d5, d7);
+    if (r == 0) return exact_bits<11, TOP_SOLID_LEVEL - 10>(s, X, Z, d5, d7);  // level 16: air
     if (r == 1) return exact_bits<0, 6>(s, X, Z, d5, d7);
     return exact_bits<6, 5>(s, X, Z, d5, d7);
 }
@@ -215,7 +215,7 @@ __device__ __forceinline__ void column_task(FastSmem& s, int q, int c, int col, 
     unsigned bits = 0;
     bool ok;
     if (forceExact) ok = false;
-    else if (r == 0) ok = screened_bits<11, 6>(w, c, col, bits);
+    else if (r == 0) ok = screened_bits<11, TOP_SOLID_LEVEL - 10>(w, c, col, bits);  // levels 11..15; 16 is air
     else if (r == 1) ok = screened_bits<0, 6>(w, c, col, bits);
     else ok = screened_bits<6, 5>(w, c, col, bits);
     if (ok) {
@@ -233,7 +233,7 @@ __device__ __forceinline__ void column_task(FastSmem& s, int q, int c, int col, 
 __device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
-    if (r == 0) return exactwarp::exact_column_warp<11, 6>(s, cx, cz);
+    if (r == 0) return exactwarp::exact_column_warp<11, TOP_SOLID_LEVEL - 10>(s, cx, cz);
     if (r == 1) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
     return exactwarp::exact_column_warp<6, 5>(s, cx, cz);
 }
