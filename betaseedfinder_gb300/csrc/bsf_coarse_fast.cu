@@ -145,7 +145,7 @@ __device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int c
 // which are left out when every converged lane of the warp is in that branch.
 __device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
     float n5 = 0.0f;
-#pragma unroll
+#pragma unroll 1  // rolled: the unrolled octaves overflow the instruction cache
     for (int o = 0; o < 16; ++o) {
         const float v = octave2f(s.perm + (ST_N5 + o) * PERM_BYTES, ax_x(s, ST_N5 + o, kx), ax_z(s, ST_N5 + o, kz)) *
                         static_cast<float>(1 << o);
@@ -159,7 +159,7 @@ __device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, i
         Fe temp, rain;
         climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
         float n4 = 0.0f;
-#pragma unroll
+#pragma unroll 1
         for (int o = 0; o < 10; ++o) {
             const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx),
                                      ax_z(s, ST_N4 + o, kz)) * static_cast<float>(1 << o);
@@ -178,44 +178,11 @@ __device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, i
 template <int Y0, int N>
 __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz, const float* shape, unsigned& bits) {
     if (shape[1] < 0.0f) return false;
-    float a1[N], a2[N], a3[N];
-    // noise1 first: per level it selects noise2, noise3 or their lerp
-#pragma unroll 1
-    for (int o = 0; o < 8; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N1 + o) * PERM_BYTES, ax_x(s, ST_N1 + o, kx), ax_z(s, ST_N1 + o, kz),
-                        s.yf[32 + o], static_cast<float>(1 << o), a1, o == 0);
-    unsigned need = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k) need |= noise_select_f(a1[k]);
-    need = __reduce_or_sync(__activemask(), need);  // warp-uniform: skip a sum no converged lane reads
-    if (need & 1u) {
-#pragma unroll 1
-        for (int o = 0; o < 16; ++o)
-            octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, ax_x(s, ST_N2 + o, kx), ax_z(s, ST_N2 + o, kz),
-                            s.yf[o], static_cast<float>(1 << o), a2, o == 0);
-    } else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) a2[k] = 0.0f;  // read by no level
-    }
-    if (need & 2u) {
-#pragma unroll 1
-        for (int o = 0; o < 16; ++o)
-            octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, ax_x(s, ST_N3 + o, kx), ax_z(s, ST_N3 + o, kz),
-                            s.yf[16 + o], static_cast<float>(1 << o), a3, o == 0);
-    } else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) a3[k] = 0.0f;  // read by no level
-    }
-    const Fe d5{shape[0], shape[1]}, d7{shape[2], shape[3]};
-    unsigned b = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const int sg = density_sign_f(Y0 + k, d5, d7, a1[k], a2[k], a3[k]);
-        if (sg == 0) return false;
-        if (sg > 0) b |= 1u << (Y0 + k);
-    }
-    bits = b;
-    return true;
+    auto oct = [&](int st, int o, float* v) {  // state st's octave o (st is also its Y-table index)
+        octave3f<Y0, N>(s.perm + st * PERM_BYTES, ax_x(s, st, kx), ax_z(s, st, kz), s.yf[st],
+                        static_cast<float>(1 << o), v, true);
+    };
+    return progressive_signs<Y0, N>(Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
 }
 
 // CT threads per CTA (and columns per tile), MINB CTAs per SM: chosen by the autotuner.

@@ -178,6 +178,14 @@ constexpr float E_N1 = octave_sum_bound(8, E_OCT3);   // noise1
 constexpr float E_N4 = octave_sum_bound(10, E_OCT2);  // noise4
 constexpr float E_N5 = octave_sum_bound(16, E_OCT2);  // noise5
 
+// Bound of a 16-octave sum taken from the largest weight down (2^15 first): the
+// per-octave terms as above, and each of the 16 adds rounds a partial sum no
+// larger than 2 * (2^16 - 1).
+__host__ __device__ constexpr float octave_sum_bound_desc(int n, float e) {
+    return static_cast<float>((1 << n) - 1) * e + U * static_cast<float>(n) * 2.0f * static_cast<float>(1 << n);
+}
+constexpr float E_N2_DESC = octave_sum_bound_desc(16, E_OCT3);
+
 // Simplex sample with exact FP64 lattice geometry and an FP32 kernel: the
 // offsets d11..d16 are FP64 (they cancel large coordinates), the falloff and
 // gradients are FP32 tracked with bounds. Returns 70*(n0+n1+n2) with its bound.
@@ -214,7 +222,8 @@ __device__ __forceinline__ float simplex_corner(float x, float z, int g, float& 
     return n.v;
 }
 
-__device__ __forceinline__ Fe simplex2f(const Gen& s, double xs, double zs) {
+// Out of line: the climate's ten octaves would otherwise inline ten copies.
+static __device__ __noinline__ Fe simplex2f(const Gen& s, double xs, double zs) {
     constexpr double F = 0.3660254037844386;
     constexpr double G = 0.21132486540518713;
     const double d5 = xs + s.a;
@@ -342,19 +351,6 @@ __device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, F
     return true;
 }
 
-// Which of noise2 / noise3 the density at one level reads (BetaTerrain173.java:
-// 812-822): d12 = (n1/10 + 1)/2 selects d10 (noise2) below 0, d11 (noise3) above
-// 1 and their lerp in between. Bit 0: noise2 may be read; bit 1: noise3 may be
-// read. The test is the one density_sign_f applies, on the same FP32 values, so
-// a noise sum that no level reads may be left out (about 57% of Stage0 column
-// tasks need only one of the two 16-octave sums).
-__device__ __forceinline__ unsigned noise_select_f(float n1) {
-    const Fe d12 = fe_scale(fe_add(fe_div(Fe{n1, E_N1}, Fe{10.0f, 0.0f}), Fe{1.0f, 0.0f}), 0.5f);
-    if (d12.v + d12.e < 0.0f) return 1u;
-    if (d12.v - d12.e > 1.0f) return 2u;
-    return 3u;
-}
-
 // Level 16 of a 17-level column is air everywhere: the top fade of
 // BetaTerrain173.java:808-830 has d13 = (float)(16 - 13) / 3.0F = 1.0 there, so
 // the density is d8 * 0.0 + -10.0 * 1.0 = -10.0 for any finite d8 (d5 >= 0.5
@@ -362,33 +358,117 @@ __device__ __forceinline__ unsigned noise_select_f(float n1) {
 // up to 15 and leave bit 16 clear.
 constexpr int TOP_SOLID_LEVEL = 15;
 
-// Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1
-// when decided, 0 when the FP64 value could have either sign.
-__device__ __forceinline__ int density_sign_f(int y, Fe d5, Fe d7, float n1, float n2, float n3) {
-    const Fe d10{n2 * (1.0f / 512.0f), E_N2 / 512.0f + fabsf(n2) * (U / 512.0f)};
-    const Fe d11{n3 * (1.0f / 512.0f), E_N2 / 512.0f + fabsf(n3) * (U / 512.0f)};
+// The parts of a level's density test that do not depend on noise2/noise3
+// (BetaTerrain173.java:808-822): the shape term d9 and the noise selector
+// d12 = (n1/10 + 1)/2, kept as which of d10 (noise2, bit 0) and d11 (noise3,
+// bit 1) the density may read and, for the lerp, d12 clamped to [0, 1].
+struct LevelTerms {
+    Fe d9, t;
+    unsigned sel;
+};
+__device__ __forceinline__ LevelTerms level_terms(int y, Fe d5, Fe d7, float n1) {
+    LevelTerms lt;
     const Fe d12 = fe_scale(fe_add(fe_div(Fe{n1, E_N1}, Fe{10.0f, 0.0f}), Fe{1.0f, 0.0f}), 0.5f);
-    Fe d8;
-    if (d12.v + d12.e < 0.0f) {
-        d8 = d10;
-    } else if (d12.v - d12.e > 1.0f) {
-        d8 = d11;
-    } else {
-        // interior (or a clamp edge): the lerp with t clamped to [0, 1] covers both sides
-        const Fe t = fe_clamp_hi(fe_clamp_lo(d12, 0.0f), 1.0f);
-        d8 = fe_add(d10, fe_mul(fe_sub(d11, d10), t));
-    }
+    // below 0 only d10 is read, above 1 only d11; in between (or at a clamp
+    // edge) the lerp with t clamped to [0, 1] covers both sides
+    lt.sel = d12.v + d12.e < 0.0f ? 1u : (d12.v - d12.e > 1.0f ? 2u : 3u);
+    lt.t = fe_clamp_hi(fe_clamp_lo(d12, 0.0f), 1.0f);
     Fe d9 = fe_div(fe_scale(fe_sub(Fe{static_cast<float>(y), 0.0f}, d7), 12.0f), d5);
     if (d9.v < 0.0f || fabsf(d9.v) <= d9.e) d9 = Fe{d9.v < 0.0f ? d9.v * 4.0f : d9.v, d9.e * 4.0f};
-    Fe d = fe_sub(d8, d9);
+    lt.d9 = d9;
+    return lt;
+}
+
+// Density sign at level y from noise sums whose noise2/noise3 carry their own
+// bounds (a partial sum: its rounding bound plus the unsummed octaves' largest
+// possible contribution). +1 / -1 when decided, 0 when either sign is possible.
+// Written without branches: it runs once per octave pair in the screened loops.
+__device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n2, Fe n3) {
+    const Fe d10{n2.v * (1.0f / 512.0f), n2.e / 512.0f + fabsf(n2.v) * (U / 512.0f)};
+    const Fe d11{n3.v * (1.0f / 512.0f), n3.e / 512.0f + fabsf(n3.v) * (U / 512.0f)};
+    const Fe mix = fe_add(d10, fe_mul(fe_sub(d11, d10), lt.t));
+    const Fe d8 = lt.sel == 1u ? d10 : (lt.sel == 2u ? d11 : mix);
+    Fe d = fe_sub(d8, lt.d9);
     if (y > 13) {
         const float d13 = static_cast<float>(y - 13) / 3.0f;  // exact as the reference's float division
         d = fe_add(fe_mul(d, Fe{1.0f - d13, 2.0f * U}), Fe{-10.0f * d13, 20.0f * U});
     }
     const float bound = 2.0f * d.e + 1.0e-6f;
-    if (d.v > bound) return 1;
-    if (d.v < -bound) return -1;
-    return 0;
+    return (d.v > bound ? 1 : 0) - (d.v < -bound ? 1 : 0);
+}
+
+// Screened signs of one column for levels [Y0, Y0+N) with noise2 and noise3
+// summed from the largest octave (weight 2^15) down, stopping once every level's
+// sign is certain, and skipping a sum that no open level of the converged lanes
+// reads (LevelTerms::sel). Octave o contributes at most 2 * 2^o (gradient dot products
+// are at most |u| + |v| <= 2 and the trilinear weights are convex), so after
+// octaves 15..o the unsummed rest is at most 2 * (2^o - 1); it is added to the
+// sums' bounds. An undecided level at the end returns false (the exact FP64 path
+// decides). oct(state, o, v) writes octave o of generator state `state`, weight
+// 2^o, for the N levels into v. All 40 octaves go through one loop body with one
+// octave evaluation in it: the unrolled octave code is large, and a body holding
+// several copies misses the instruction cache on every iteration.
+template <int Y0, int N, typename OctFn>
+__device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsigned& bits) {
+    float a1[N], a2[N], a3[N];
+    LevelTerms lt[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) a1[k] = a2[k] = a3[k] = 0.0f;  // a skipped sum is read by no open level
+    unsigned open = (1u << N) - 1u, pos = 0;
+    // steps 0..7: noise1 octaves 0..7 (the reference's order, 0.0 + first term
+    // being exact); then for o = 15..0 two steps, noise2 and noise3 octave o
+#pragma unroll 1
+    for (int j = 0; j < 40; ++j) {
+        const bool n1 = j < 8;
+        const int o = n1 ? j : 15 - ((j - 8) >> 1);
+        const bool third = !n1 && ((j - 8) & 1);
+        bool run = true;
+        if (!n1) {
+            if (j == 8) {
+#pragma unroll
+                for (int k = 0; k < N; ++k) lt[k] = level_terms(Y0 + k, d5, d7, a1[k]);
+            }
+            unsigned need = 0;
+#pragma unroll
+            for (int k = 0; k < N; ++k) need |= ((open >> k) & 1u) ? lt[k].sel : 0u;
+            // Any superset of this lane's own need is correct, so the converged
+            // lanes' union serves them all and keeps the octave loads warp-uniform.
+            need = __reduce_or_sync(__activemask(), need);
+            run = (need & (third ? 2u : 1u)) != 0;
+        }
+        if (run) {  // the one octave evaluation of the loop body
+            float v[N];
+            oct((n1 ? ST_N1 : (third ? ST_N3 : ST_N2)) + o, o, v);
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                if (n1) a1[k] = a1[k] + v[k];
+                else if (third) a3[k] = a3[k] + v[k];
+                else a2[k] = a2[k] + v[k];
+            }
+        }
+        if (!third) continue;
+        const float err = E_N2_DESC + 2.0f * static_cast<float>((1 << o) - 1);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            // a closed level keeps its sign: a later interval may straddle 0 again
+            const int sg = density_sign_lt(Y0 + k, lt[k], Fe{a2[k], err}, Fe{a3[k], err});
+            const bool was = (open >> k) & 1u;
+            pos |= (was && sg > 0) ? 1u << (Y0 + k) : 0u;
+            open &= sg != 0 ? ~(1u << k) : ~0u;
+        }
+        // The converged lanes leave together: a lane that ran ahead into its
+        // next task would split the warp into two instruction streams.
+        if (__all_sync(__activemask(), open == 0)) break;
+    }
+    if (open) return false;
+    bits = pos;
+    return true;
+}
+
+// Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1
+// when decided, 0 when the FP64 value could have either sign.
+__device__ __forceinline__ int density_sign_f(int y, Fe d5, Fe d7, float n1, float n2, float n3) {
+    return density_sign_lt(y, level_terms(y, d5, d7, n1), Fe{n2, E_N2}, Fe{n3, E_N2});
 }
 
 }  // namespace screen

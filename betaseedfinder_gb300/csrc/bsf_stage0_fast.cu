@@ -63,6 +63,7 @@ struct FastSmem {
     std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
     std::uint32_t fb[FB_CAP];             // (range << 13 | slot << 11 | centre << 8 | column)
     int taskCount, fbCount, screened, fallbacks;
+    int cursor[3];                        // next unclaimed task of the P20, Upper and Lower phases
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
               "uint4 copies into perm and out of axf need 16-byte alignment");
@@ -160,18 +161,17 @@ __device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, 
     column_coords(c, col, cx, cz, kx, kz);
     Fe temp, rain;
     climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
+    // noise4 octaves 0..9, then noise5 octaves 0..15, through one loop body (code size)
     float n4 = 0.0f, n5 = 0.0f;
-#pragma unroll
-    for (int o = 0; o < 10; ++o) {
-        const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, axis_of(s, ST_N4 + o, 0, kx),
-                                 axis_of(s, ST_N4 + o, 1, kz)) * static_cast<float>(1 << o);
-        n4 = o == 0 ? v : n4 + v;
-    }
-#pragma unroll
-    for (int o = 0; o < 16; ++o) {
-        const float v = octave2f(s.perm + (ST_N5 + o) * PERM_BYTES, axis_of(s, ST_N5 + o, 0, kx),
-                                 axis_of(s, ST_N5 + o, 1, kz)) * static_cast<float>(1 << o);
-        n5 = o == 0 ? v : n5 + v;
+#pragma unroll 1
+    for (int i = 0; i < 26; ++i) {
+        static_assert(ST_N5 == ST_N4 + 10, "noise5 states follow noise4's");
+        const int st = ST_N4 + i;
+        const int o = i < 10 ? i : i - 10;
+        const float v = octave2f(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz)) *
+                        static_cast<float>(1 << o);
+        if (i < 10) n4 = n4 + v;  // 0.0f + first term is exact
+        else n5 = n5 + v;
     }
     return column_shape_f(temp, rain, Fe{n4, E_N4}, Fe{n5, E_N5}, d5, d7);
 }
@@ -183,28 +183,11 @@ __device__ __noinline__ bool screened_bits(const WorldSmem& s, int c, int col, u
     if (!screened_shape(s, c, col, d5, d7)) return false;
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
-    float a1[N], a2[N], a3[N];
-#pragma unroll 1
-    for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N2 + o) * PERM_BYTES, axis_of(s, ST_N2 + o, 0, kx), axis_of(s, ST_N2 + o, 1, kz),
-                        s.yf[o], static_cast<float>(1 << o), a2, o == 0);
-#pragma unroll 1
-    for (int o = 0; o < 16; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N3 + o) * PERM_BYTES, axis_of(s, ST_N3 + o, 0, kx), axis_of(s, ST_N3 + o, 1, kz),
-                        s.yf[16 + o], static_cast<float>(1 << o), a3, o == 0);
-#pragma unroll 1
-    for (int o = 0; o < 8; ++o)
-        octave3f<Y0, N>(s.perm + (ST_N1 + o) * PERM_BYTES, axis_of(s, ST_N1 + o, 0, kx), axis_of(s, ST_N1 + o, 1, kz),
-                        s.yf[32 + o], static_cast<float>(1 << o), a1, o == 0);
-    unsigned b = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-        const int sg = density_sign_f(Y0 + k, d5, d7, a1[k], a2[k], a3[k]);
-        if (sg == 0) return false;
-        if (sg > 0) b |= 1u << (Y0 + k);
-    }
-    bits = b;
-    return true;
+    auto oct = [&](int st, int o, float* v) {  // state st's octave o (st is also its Y-table index)
+        octave3f<Y0, N>(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz), s.yf[st],
+                        static_cast<float>(1 << o), v, true);
+    };
+    return progressive_signs<Y0, N>(d5, d7, oct, bits);
 }
 
 // One column task of world slot q: screened, else queued for (or, when the list
@@ -236,6 +219,22 @@ __device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col
     if (r == 0) return exactwarp::exact_column_warp<11, TOP_SOLID_LEVEL - 10>(s, cx, cz);
     if (r == 1) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
     return exactwarp::exact_column_warp<6, 5>(s, cx, cz);
+}
+
+// A phase's tasks [0, total) handed out 32 at a time to whichever warp asks
+// next: a screened task stops as soon as its signs are certain, so task costs
+// vary, and a fixed split would leave the CTA waiting at the phase's barrier for
+// its slowest warp. Every lane of the warp calls it.
+template <typename F>
+__device__ __forceinline__ void warp_chunks(int* cursor, int total, F body) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(cursor, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        if (base + lane < total) body(base + lane);
+    }
 }
 
 // Fallback pass: one warp per undecided column task.
@@ -294,7 +293,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             const int c = tid & 7;
             w.p20[c] = 0; w.upper[c] = 0; w.high[c] = 0; w.gate[c] = 0;
         }
-        if (tid == 0) { s.fbCount = 0; s.taskCount = 0; }
+        if (tid == 0) { s.fbCount = 0; s.taskCount = 0; s.cursor[0] = s.cursor[1] = s.cursor[2] = 0; }
         for (int k = tid; k < nw * 8 * 256; k += FT) (&s.w[k >> 11].mask17[0][0])[k & 2047] = 0;
         __syncthreads();
         if (tid < OCT3 * nw) {
@@ -321,11 +320,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         const int p20Tasks = centers * 64;
-        for (int t = tid; t < nw * p20Tasks; t += FT) {
+        warp_chunks(&s.cursor[0], nw * p20Tasks, [&](int t) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
             column_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true, fs.forceExact);
-        }
+        });
         run_fallbacks(s);
         for (int t = tid; t < nw * p20Tasks; t += FT) {
             const int q = t / p20Tasks, u = t % p20Tasks;
@@ -349,10 +348,10 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
         const int upperUnits = s.taskCount;
-        for (int t = tid; t < upperUnits * 192; t += FT) {
+        warp_chunks(&s.cursor[1], upperUnits * 192, [&](int t) {
             const int e = s.tasks[t / 192];
             column_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], 0, true, fs.forceExact);
-        }
+        });
         run_fallbacks(s);
         for (int t = tid; t < upperUnits * 192; t += FT) {
             const int e = s.tasks[t / 192];
@@ -373,11 +372,15 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         }
         __syncthreads();
         // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239).
-        const int lowerTasks = s.taskCount * 2;
-        for (int t = tid; t < lowerTasks; t += FT) {
-            const int e = s.tasks[t >> 1];
-            column_task(s, e >> 11, (e >> 8) & 7, e & 255, (t & 1) ? 2 : 1, false, fs.forceExact);
-        }
+        // Task t covers column (t >> 6) * 32 + (t & 31), levels 0..5 when bit 5 of t is clear and
+        // 6..10 when it is set, so each claimed chunk of 32 runs one level range.
+        const int lowerCols = s.taskCount;
+        warp_chunks(&s.cursor[2], ((lowerCols + 31) & ~31) * 2, [&](int t) {
+            const int i = ((t >> 6) << 5) + (t & 31);
+            if (i >= lowerCols) return;
+            const int e = s.tasks[i];
+            column_task(s, e >> 11, (e >> 8) & 7, e & 255, (t & 32) ? 2 : 1, false, fs.forceExact);
+        });
         run_fallbacks(s);
         // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
         for (int k = tid; k < nw * 8 * 256; k += FT)
