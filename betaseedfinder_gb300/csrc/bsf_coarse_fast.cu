@@ -106,9 +106,9 @@ __device__ unsigned exact_bits(const CoarseSmem& s, double X, double Z, double d
 
 // Exact FP64 column for Y range r by one whole warp (fallback pass).
 __device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int cz, int r) {
-    if (r == 0) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
-    if (r == 1) return exactwarp::exact_column_warp<6, 6>(s, cx, cz);
-    return exactwarp::exact_column_warp<12, TOP_SOLID_LEVEL - 11>(s, cx, cz);  // level 16: air
+    // level 16 is air
+    const int y0 = r == 0 ? 0 : (r == 1 ? 6 : 12), n = r == 2 ? TOP_SOLID_LEVEL - 11 : 6;
+    return exactwarp::exact_column_warp(s, cx, cz, y0, n);
 }
 
 // Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,16), level 16 is air) by one

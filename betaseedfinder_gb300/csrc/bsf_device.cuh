@@ -129,25 +129,63 @@ __device__ __forceinline__ void build_yaxis(double sy, double b, YEntry* out) {
     }
 }
 
+// X/Z lattice of one 3D octave column (x = xs + a, z = zs + c already scaled).
+struct Lattice3 {
+    double x, x1, xf, z, z1, zf;
+    int zi, xp0, xp1;
+};
+__device__ __forceinline__ Lattice3 lattice3(const Gen& g, double xs, double zs) {
+    Lattice3 L;
+    double x = xs + g.a;
+    const int fx = jfloor(x);
+    const int xi = fx & 255;
+    x -= static_cast<double>(fx);
+    L.x = x;
+    L.xf = fade(x);
+    double z = zs + g.c;
+    const int fz = jfloor(z);
+    L.zi = fz & 255;
+    z -= static_cast<double>(fz);
+    L.z = z;
+    L.zf = fade(z);
+    L.x1 = x - 1.0;
+    L.z1 = z - 1.0;
+    L.xp0 = P(g.p, xi);
+    L.xp1 = P(g.p, xi + 1);
+    return L;
+}
+
+// Corner gradients of the Y cell of sample e, lerped along X.
+__device__ __forceinline__ void cell_corners(const Gen& g, const Lattice3& L, const YEntry& e, double& c00,
+                                             double& c01, double& c10, double& c11) {
+    const double y = e.cellFrac;
+    const double y1 = y - 1.0;
+    const int p0 = L.xp0 + e.yi;
+    const int p00 = P(g.p, p0) + L.zi;
+    const int p01 = P(g.p, p0 + 1) + L.zi;
+    const int p1 = L.xp1 + e.yi;
+    const int p10 = P(g.p, p1) + L.zi;
+    const int p11 = P(g.p, p1 + 1) + L.zi;
+    c00 = lerp(L.xf, grad3(P(g.p, p00), L.x, y, L.z), grad3(P(g.p, p10), L.x1, y, L.z));
+    c01 = lerp(L.xf, grad3(P(g.p, p01), L.x, y1, L.z), grad3(P(g.p, p11), L.x1, y1, L.z));
+    c10 = lerp(L.xf, grad3(P(g.p, p00 + 1), L.x, y, L.z1), grad3(P(g.p, p10 + 1), L.x1, y, L.z1));
+    c11 = lerp(L.xf, grad3(P(g.p, p01 + 1), L.x, y1, L.z1), grad3(P(g.p, p11 + 1), L.x1, y1, L.z1));
+}
+
+// weight * noise at sample e from its cell's corners.
+__device__ __forceinline__ double cell_sample(const Lattice3& L, const YEntry& e, double c00, double c01, double c10,
+                                              double c11, double weight) {
+    const double r0 = lerp(e.fade, c00, c01);
+    const double r1 = lerp(e.fade, c10, c11);
+    return lerp(L.zf, r0, r1) * weight;
+}
+
 // Adds weight * noise for samples y in [Y0, Y0+N) of one 3D octave column
 // (x = xs + a, z = zs + c already scaled), reusing corner gradients per Y cell.
 template <int Y0, int N>
 __device__ __forceinline__ void octave3_column(const Gen& g, double xs, double zs, const YEntry* ya,
                                                double weight, double* acc, bool first) {
-    double x = xs + g.a;
-    const int fx = jfloor(x);
-    const int xi = fx & 255;
-    x -= static_cast<double>(fx);
-    const double xf = fade(x);
-    double z = zs + g.c;
-    const int fz = jfloor(z);
-    const int zi = fz & 255;
-    z -= static_cast<double>(fz);
-    const double zf = fade(z);
-    const double x1 = x - 1.0;
-    const double z1 = z - 1.0;
-    const int xp0 = P(g.p, xi);
-    const int xp1 = P(g.p, xi + 1);
+    const Lattice3 L = lattice3(g, xs, zs);
     int activeCell = -1;
     double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
 #pragma unroll
@@ -155,22 +193,9 @@ __device__ __forceinline__ void octave3_column(const Gen& g, double xs, double z
         const YEntry e = ya[Y0 + k];
         if (e.cell != activeCell) {
             activeCell = e.cell;
-            const double y = e.cellFrac;
-            const double y1 = y - 1.0;
-            const int p0 = xp0 + e.yi;
-            const int p00 = P(g.p, p0) + zi;
-            const int p01 = P(g.p, p0 + 1) + zi;
-            const int p1 = xp1 + e.yi;
-            const int p10 = P(g.p, p1) + zi;
-            const int p11 = P(g.p, p1 + 1) + zi;
-            c00 = lerp(xf, grad3(P(g.p, p00), x, y, z), grad3(P(g.p, p10), x1, y, z));
-            c01 = lerp(xf, grad3(P(g.p, p01), x, y1, z), grad3(P(g.p, p11), x1, y1, z));
-            c10 = lerp(xf, grad3(P(g.p, p00 + 1), x, y, z1), grad3(P(g.p, p10 + 1), x1, y, z1));
-            c11 = lerp(xf, grad3(P(g.p, p01 + 1), x, y1, z1), grad3(P(g.p, p11 + 1), x1, y1, z1));
+            cell_corners(g, L, e, c00, c01, c10, c11);
         }
-        const double r0 = lerp(e.fade, c00, c01);
-        const double r1 = lerp(e.fade, c10, c11);
-        const double v = lerp(zf, r0, r1) * weight;
+        const double v = cell_sample(L, e, c00, c01, c10, c11, weight);
         acc[k] = first ? 0.0 + v : acc[k] + v;
     }
 }

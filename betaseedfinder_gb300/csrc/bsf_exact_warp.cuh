@@ -64,25 +64,42 @@ __device__ __forceinline__ void y_entries(const S& s, int state, YEntry* ya) {
     build_yaxis(sy, s.off[state][1], ya);
 }
 
-// One 3D octave column's terms (octave3_column with the sums left out).
-template <int Y0, int N, typename S>
+// Most levels one column task covers (the screened kernels' ranges have 4 to 6).
+constexpr int MAX_LEVELS = 6;
+
+// One 3D octave column's terms for levels [y0, y0+n): octave3_column's
+// arithmetic with the sums left out, in a rolled loop over the levels.
+template <typename S>
 __device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int state, double sc0, int o, double X,
-                                             double Z, double* out) {
+                                             double Z, int y0, int n, double* out) {
     const double amp = 1.0 / static_cast<double>(1 << o);
     const double sc = sc0 * amp;
     YEntry ya[17];
     y_entries(s, state, ya);
-    double acc[N];
-    octave3_column<Y0, N>(t(state), X * sc, Z * sc, ya, 1.0 / amp, acc, true);
-#pragma unroll
-    for (int k = 0; k < N; ++k) out[k] = acc[k];  // 0.0 + v: the first-octave form, same sum
+    const Gen g = t(state);
+    const Lattice3 L = lattice3(g, X * sc, Z * sc);
+    const double weight = 1.0 / amp;
+    int activeCell = -1;
+    double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
+        const YEntry e = ya[y0 + k];
+        if (e.cell != activeCell) {
+            activeCell = e.cell;
+            cell_corners(g, L, e, c00, c01, c10, c11);
+        }
+        out[k] = 0.0 + cell_sample(L, e, c00, c01, c10, c11, weight);  // the first-octave form, same sum
+    }
 }
 
-// Exact density signs of the column at coarse (cx, cz) for levels [Y0, Y0+N),
-// climate sampled at block (4cx+2, 4cz+2). All 32 lanes must call it with the
-// same arguments; every lane returns the same bits.
-template <int Y0, int N, typename S>
-__device__ unsigned exact_column_warp(const S& s, int cx, int cz) {
+// Exact density signs of the column at coarse (cx, cz) for levels [y0, y0+n),
+// n <= MAX_LEVELS, climate sampled at block (4cx+2, 4cz+2). All 32 lanes must
+// call it with the same arguments; every lane returns the same bits. The levels
+// are runtime values and every loop has one call site: the path is rare, and
+// unrolled or instantiated per level range its FP64 code (hundreds of KB)
+// streamed through the instruction cache on each call.
+template <typename S>
+__device__ unsigned exact_column_warp(const S& s, int cx, int cz, int y0, int n) {
     const int lane = threadIdx.x & 31;
     GenTable t;
     t.perm = s.perm;
@@ -90,8 +107,14 @@ __device__ unsigned exact_column_warp(const S& s, int cx, int cz) {
     const double X = static_cast<double>(cx), Z = static_cast<double>(cz);
     const double BX = static_cast<double>(cx * 4 + 2), BZ = static_cast<double>(cz * 4 + 2);
     // shape: 36 terms over two rounds of lanes
-    const double s0 = shape_term(t, lane, X, Z, BX, BZ);
-    const double s1 = lane < 4 ? shape_term(t, 32 + lane, X, Z, BX, BZ) : 0.0;
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll 1
+    for (int r = 0; r < 2; ++r) {
+        const int i = r * 32 + lane;
+        const double v = i < 36 ? shape_term(t, i, X, Z, BX, BZ) : 0.0;
+        if (r == 0) s0 = v;
+        else s1 = v;
+    }
     double raw[3];
     raw[0] = ordered_sum(s0, 0, 4);
     raw[1] = ordered_sum(s0, 4, 4);
@@ -105,21 +128,24 @@ __device__ unsigned exact_column_warp(const S& s, int cx, int cz) {
     double d5, d7;
     column_shape(temperature, rain, n4, n5, d5, d7);
     // 3D octaves: lanes 0-15 noise2, 16-31 noise3, then lanes 0-7 noise1
-    double tA[N], tB[N];
-    if (lane < 16) octave_terms<Y0, N>(s, t, ST_N2 + lane, NOISE_XZ, lane, X, Z, tA);
-    else octave_terms<Y0, N>(s, t, ST_N3 + lane - 16, NOISE_XZ, lane - 16, X, Z, tA);
-    if (lane < 8) octave_terms<Y0, N>(s, t, ST_N1 + lane, NOISE_XZ / 80.0, lane, X, Z, tB);
-    else {
-#pragma unroll
-        for (int k = 0; k < N; ++k) tB[k] = 0.0;
+    double tA[MAX_LEVELS], tB[MAX_LEVELS];
+#pragma unroll 1
+    for (int r = 0; r < 2; ++r) {
+        double* out = r == 0 ? tA : tB;
+        const int st = r == 0 ? (lane < 16 ? ST_N2 + lane : ST_N3 + lane - 16) : ST_N1 + lane;
+        if (r == 0 || lane < 8) {
+            octave_terms(s, t, st, r == 0 ? NOISE_XZ : NOISE_XZ / 80.0, r == 0 ? (lane & 15) : lane, X, Z, y0, n, out);
+        } else {
+            for (int k = 0; k < n; ++k) out[k] = 0.0;
+        }
     }
     unsigned bits = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
+#pragma unroll 1
+    for (int k = 0; k < n; ++k) {
         const double n2 = ordered_sum(tA[k], 0, 16);
         const double n3 = ordered_sum(tA[k], 16, 16);
         const double n1 = ordered_sum(tB[k], 0, 8);
-        if (density_at(Y0 + k, d5, d7, n1, n2, n3) > 0.0) bits |= 1u << (Y0 + k);
+        if (density_at(y0 + k, d5, d7, n1, n2, n3) > 0.0) bits |= 1u << (y0 + k);
     }
     return bits;
 }

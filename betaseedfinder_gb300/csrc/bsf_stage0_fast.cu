@@ -176,11 +176,10 @@ __device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, 
     return column_shape_f(temp, rain, Fe{n4, E_N4}, Fe{n5, E_N5}, d5, d7);
 }
 
-// Screened signs of one column for levels [Y0, Y0+N); false when undecided.
+// Screened signs of one column for levels [Y0, Y0+N) given its shape; false
+// when undecided.
 template <int Y0, int N>
-__device__ __noinline__ bool screened_bits(const WorldSmem& s, int c, int col, unsigned& bits) {
-    Fe d5, d7;
-    if (!screened_shape(s, c, col, d5, d7)) return false;
+__device__ __noinline__ bool screened_range(const WorldSmem& s, int c, int col, Fe d5, Fe d7, unsigned& bits) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     auto oct = [&](int st, int o, float* v) {  // state st's octave o (st is also its Y-table index)
@@ -190,35 +189,51 @@ __device__ __noinline__ bool screened_bits(const WorldSmem& s, int c, int col, u
     return progressive_signs<Y0, N>(d5, d7, oct, bits);
 }
 
-// One column task of world slot q: screened, else queued for (or, when the list
-// is full, given) the exact path.
-__device__ __forceinline__ void column_task(FastSmem& s, int q, int c, int col, int r, bool store, bool forceExact) {
-    WorldSmem& w = s.w[q];
-    atomicAdd(&s.screened, 1);
-    unsigned bits = 0;
-    bool ok;
-    if (forceExact) ok = false;
-    else if (r == 0) ok = screened_bits<11, TOP_SOLID_LEVEL - 10>(w, c, col, bits);  // levels 11..15; 16 is air
-    else if (r == 1) ok = screened_bits<0, 6>(w, c, col, bits);
-    else ok = screened_bits<6, 5>(w, c, col, bits);
-    if (ok) {
-        if (store) w.mask17[c][col] = bits;
-        else if (bits) atomicOr(&w.mask17[c][col], bits);
-        return;
-    }
+// A column range the screen left undecided: queued for the exact path, or,
+// when the list is full, given it here.
+__device__ __forceinline__ void fallback_task(FastSmem& s, int q, int c, int col, int r) {
     atomicAdd(&s.fallbacks, 1);
     const int slot = atomicAdd(&s.fbCount, 1);
     if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
-    else atomicOr(&w.mask17[c][col], exact_task(w, c, col, r));
+    else atomicOr(&s.w[q].mask17[c][col], exact_task(s.w[q], c, col, r));
+}
+
+// P20 / Upper column task of world slot q: levels 11..15 (16 is air).
+__device__ __forceinline__ void upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+    WorldSmem& w = s.w[q];
+    atomicAdd(&s.screened, 1);
+    Fe d5, d7;
+    unsigned bits = 0;
+    if (!forceExact && screened_shape(w, c, col, d5, d7) &&
+        screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, d5, d7, bits)) {
+        w.mask17[c][col] = bits;
+        return;
+    }
+    fallback_task(s, q, c, col, 0);
+}
+
+// Lower column task: levels 0..5 and 6..10 (two screened tasks) on one shape.
+__device__ __forceinline__ void lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+    WorldSmem& w = s.w[q];
+    atomicAdd(&s.screened, 2);
+    Fe d5, d7;
+    const bool shaped = !forceExact && screened_shape(w, c, col, d5, d7);
+    unsigned lo = 0, hi = 0;
+    const bool okLo = shaped && screened_range<0, 6>(w, c, col, d5, d7, lo);
+    const bool okHi = shaped && screened_range<6, 5>(w, c, col, d5, d7, hi);
+    const unsigned bits = (okLo ? lo : 0u) | (okHi ? hi : 0u);
+    if (bits) atomicOr(&w.mask17[c][col], bits);
+    if (!okLo) fallback_task(s, q, c, col, 1);
+    if (!okHi) fallback_task(s, q, c, col, 2);
 }
 
 // Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
 __device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
-    if (r == 0) return exactwarp::exact_column_warp<11, TOP_SOLID_LEVEL - 10>(s, cx, cz);
-    if (r == 1) return exactwarp::exact_column_warp<0, 6>(s, cx, cz);
-    return exactwarp::exact_column_warp<6, 5>(s, cx, cz);
+    // levels 11..15 (16 is air), 0..5 or 6..10
+    const int y0 = r == 0 ? 11 : (r == 1 ? 0 : 6), n = r == 0 ? TOP_SOLID_LEVEL - 10 : (r == 1 ? 6 : 5);
+    return exactwarp::exact_column_warp(s, cx, cz, y0, n);
 }
 
 // A phase's tasks [0, total) handed out 32 at a time to whichever warp asks
@@ -323,7 +338,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         warp_chunks(&s.cursor[0], nw * p20Tasks, [&](int t) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
-            column_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], 0, true, fs.forceExact);
+            upper_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], fs.forceExact);
         });
         run_fallbacks(s);
         for (int t = tid; t < nw * p20Tasks; t += FT) {
@@ -350,7 +365,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int upperUnits = s.taskCount;
         warp_chunks(&s.cursor[1], upperUnits * 192, [&](int t) {
             const int e = s.tasks[t / 192];
-            column_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], 0, true, fs.forceExact);
+            upper_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], fs.forceExact);
         });
         run_fallbacks(s);
         for (int t = tid; t < upperUnits * 192; t += FT) {
@@ -371,15 +386,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             }
         }
         __syncthreads();
-        // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239).
-        // Task t covers column (t >> 6) * 32 + (t & 31), levels 0..5 when bit 5 of t is clear and
-        // 6..10 when it is set, so each claimed chunk of 32 runs one level range.
-        const int lowerCols = s.taskCount;
-        warp_chunks(&s.cursor[2], ((lowerCols + 31) & ~31) * 2, [&](int t) {
-            const int i = ((t >> 6) << 5) + (t & 31);
-            if (i >= lowerCols) return;
+        // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239)
+        // that share the column's shape.
+        warp_chunks(&s.cursor[2], s.taskCount, [&](int i) {
             const int e = s.tasks[i];
-            column_task(s, e >> 11, (e >> 8) & 7, e & 255, (t & 32) ? 2 : 1, false, fs.forceExact);
+            lower_task(s, e >> 11, (e >> 8) & 7, e & 255, fs.forceExact);
         });
         run_fallbacks(s);
         // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
