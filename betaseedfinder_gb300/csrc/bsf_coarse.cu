@@ -51,7 +51,7 @@ __device__ void build_ytabs(LatticeSmem& s) {
     const int o = threadIdx.x;
     if (o < OCT3) {
         const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
-        const double amp = 1.0 / static_cast<double>(1 << k);
+        const double amp = exp2_neg(k);
         const double sy = o < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
         build_yaxis(sy, s.off[o][1], s.ytab[o]);
     }

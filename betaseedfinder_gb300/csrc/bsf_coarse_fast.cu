@@ -55,11 +55,12 @@ __device__ __forceinline__ GenTable gtab(const CoarseSmem& s) {
 }
 
 __device__ __forceinline__ double octave_scale(int o) {
-    if (o < 16) return NOISE_XZ / static_cast<double>(1 << o);
-    if (o < 32) return NOISE_XZ / static_cast<double>(1 << (o - 16));
-    if (o < 40) return (NOISE_XZ / 80.0) / static_cast<double>(1 << (o - 32));
-    if (o < 50) return 1.121 / static_cast<double>(1 << (o - 40));
-    return 200.0 / static_cast<double>(1 << (o - 50));
+    // base / 2^k, the scaling exact either way
+    if (o < 16) return NOISE_XZ * exp2_neg(o);
+    if (o < 32) return NOISE_XZ * exp2_neg(o - 16);
+    if (o < 40) return (NOISE_XZ / 80.0) * exp2_neg(o - 32);
+    if (o < 50) return 1.121 * exp2_neg(o - 40);
+    return 200.0 * exp2_neg(o - 50);
 }
 
 __device__ __forceinline__ AxisF ax_x(const CoarseSmem& s, int o, int k) {
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
         if (tid < OCT3) {
             const int o = tid;
             const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
-            const double amp = 1.0 / static_cast<double>(1 << k);
+            const double amp = exp2_neg(k);
             const double sy = o < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
             YEntry ya[17];
             build_yaxis(sy, s.off[o][1], ya);

@@ -51,6 +51,14 @@ __device__ __forceinline__ int jfloor(double v) {
     return v < static_cast<double>(i) ? i - 1 : i;
 }
 
+// 2^-k for 0 <= k <= 1022, built from its bits. x * exp2_neg(k) equals the
+// IEEE quotient x / 2^k exactly (both are the exact scaling while the result
+// stays normal) without an FP64 division, which GB300's narrow FP64 pipe runs
+// as a long iteration.
+__device__ __forceinline__ double exp2_neg(int k) {
+    return __longlong_as_double(static_cast<long long>(1023 - k) << 52);
+}
+
 __device__ __forceinline__ double fade(double v) {
     return v * v * v * (v * (v * 6.0 - 15.0) + 10.0);
 }

@@ -49,9 +49,9 @@ __device__ __forceinline__ double shape_term(const GenTable& t, int i, double X,
     }
     const bool n4 = i < 20;
     const int o = n4 ? i - 10 : i - 20;
-    const double amp = 1.0 / static_cast<double>(1 << o);  // exact, as amp /= 2.0 per octave
+    const double amp = exp2_neg(o);  // exact, as amp /= 2.0 per octave
     const double sc = (n4 ? 1.121 : 200.0) * amp;
-    return octave2(t((n4 ? ST_N4 : ST_N5) + o), X * sc, Z * sc) * (1.0 / amp);
+    return octave2(t((n4 ? ST_N4 : ST_N5) + o), X * sc, Z * sc) * static_cast<double>(1 << o);  // 1 / amp
 }
 
 // FP64 Y axis of 3D octave state (0..39): the legacy per-cell Y entries of
@@ -59,7 +59,7 @@ __device__ __forceinline__ double shape_term(const GenTable& t, int i, double X,
 template <typename S>
 __device__ __forceinline__ void y_entries(const S& s, int state, YEntry* ya) {
     const int k = state < 16 ? state : (state < 32 ? state - 16 : state - 32);
-    const double amp = 1.0 / static_cast<double>(1 << k);
+    const double amp = exp2_neg(k);
     const double sy = state < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
     build_yaxis(sy, s.off[state][1], ya);
 }
@@ -72,13 +72,13 @@ constexpr int MAX_LEVELS = 6;
 template <typename S>
 __device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int state, double sc0, int o, double X,
                                              double Z, int y0, int n, double* out) {
-    const double amp = 1.0 / static_cast<double>(1 << o);
+    const double amp = exp2_neg(o);
     const double sc = sc0 * amp;
     YEntry ya[17];
     y_entries(s, state, ya);
     const Gen g = t(state);
     const Lattice3 L = lattice3(g, X * sc, Z * sc);
-    const double weight = 1.0 / amp;
+    const double weight = static_cast<double>(1 << o);  // 1 / amp, exact
     int activeCell = -1;
     double c00 = 0.0, c01 = 0.0, c10 = 0.0, c11 = 0.0;
 #pragma unroll 1

@@ -213,7 +213,7 @@ __device__ __forceinline__ void build_ytabs(WorldSmem& w) {
     const int o = threadIdx.x;
     if (o < OCT3) {
         const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
-        const double amp = 1.0 / static_cast<double>(1 << k);  // exact power of two
+        const double amp = exp2_neg(k);  // exact power of two
         build_yaxis(octave_sy(o, amp), w.off[o][1], w.ytab[o]);
     }
 }

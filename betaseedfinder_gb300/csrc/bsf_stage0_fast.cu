@@ -76,11 +76,12 @@ __device__ __forceinline__ GenTable gtab(const WorldSmem& s) {
 }
 
 __device__ __forceinline__ double octave_scale(int o) {
-    if (o < 16) return NOISE_XZ / static_cast<double>(1 << o);
-    if (o < 32) return NOISE_XZ / static_cast<double>(1 << (o - 16));
-    if (o < 40) return (NOISE_XZ / 80.0) / static_cast<double>(1 << (o - 32));
-    if (o < 50) return 1.121 / static_cast<double>(1 << (o - 40));
-    return 200.0 / static_cast<double>(1 << (o - 50));
+    // base / 2^k, the scaling exact either way
+    if (o < 16) return NOISE_XZ * exp2_neg(o);
+    if (o < 32) return NOISE_XZ * exp2_neg(o - 16);
+    if (o < 40) return (NOISE_XZ / 80.0) * exp2_neg(o - 32);
+    if (o < 50) return 1.121 * exp2_neg(o - 40);
+    return 200.0 * exp2_neg(o - 50);
 }
 
 __device__ __forceinline__ AxisF axis_of(const WorldSmem& s, int o, int a, int k) {
@@ -314,7 +315,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         if (tid < OCT3 * nw) {
             const int q = tid / OCT3, o = tid % OCT3;
             const int k = o < 16 ? o : (o < 32 ? o - 16 : o - 32);
-            const double amp = 1.0 / static_cast<double>(1 << k);
+            const double amp = exp2_neg(k);
             const double sy = o < 32 ? NOISE_Y * amp : (NOISE_Y / 160.0) * amp;
             YEntry ya[17];
             build_yaxis(sy, s.w[q].off[o][1], ya);
