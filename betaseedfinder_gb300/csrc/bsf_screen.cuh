@@ -379,34 +379,42 @@ __device__ __forceinline__ LevelTerms level_terms(int y, Fe d5, Fe d7, float n1)
     return lt;
 }
 
-// Density sign at level y from noise sums whose noise2/noise3 carry their own
-// bounds (a partial sum: its rounding bound plus the unsummed octaves' largest
-// possible contribution). +1 / -1 when decided, 0 when either sign is possible.
+// Density sign at level y from noise sums with bounds: +1 / -1 when decided, 0
+// when either sign is possible. n2 / n3 may be partial sums whose unsummed
+// octaves add at most `rest` to each (an exact bound, kept apart from the FP32
+// error model): the density is d8 - d9 with d8 a convex combination of
+// n2/512 and n3/512 (d10, d11 or their lerp with t in [0, 1]), so those
+// octaves move it by at most rest / 512 times the top fade's slope (1 - d13
+// above level 13, else 1). That term is not doubled like the model's bound.
 // Written without branches: it runs once per octave pair in the screened loops.
-__device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n2, Fe n3) {
+__device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n2, Fe n3, float rest = 0.0f) {
     const Fe d10{n2.v * (1.0f / 512.0f), n2.e / 512.0f + fabsf(n2.v) * (U / 512.0f)};
     const Fe d11{n3.v * (1.0f / 512.0f), n3.e / 512.0f + fabsf(n3.v) * (U / 512.0f)};
     const Fe mix = fe_add(d10, fe_mul(fe_sub(d11, d10), lt.t));
     const Fe d8 = lt.sel == 1u ? d10 : (lt.sel == 2u ? d11 : mix);
     Fe d = fe_sub(d8, lt.d9);
+    float slope = 1.0f;
     if (y > 13) {
         const float d13 = static_cast<float>(y - 13) / 3.0f;  // exact as the reference's float division
         d = fe_add(fe_mul(d, Fe{1.0f - d13, 2.0f * U}), Fe{-10.0f * d13, 20.0f * U});
+        slope = 1.0f - d13;
     }
-    const float bound = 2.0f * d.e + 1.0e-6f;
+    // (1 + 2^-10) covers the FP32 rounding of the rest term itself
+    const float bound = 2.0f * d.e + 1.0e-6f + rest * (slope / 512.0f) * (1.0f + 1.0f / 1024.0f);
     return (d.v > bound ? 1 : 0) - (d.v < -bound ? 1 : 0);
 }
 
 // Screened signs of one column for levels [Y0, Y0+N) with noise2 and noise3
-// summed from the largest octave (weight 2^15) down, stopping once every level's
-// sign is certain, and skipping a sum that no open level of the converged lanes
-// reads (LevelTerms::sel). Octave o contributes at most 2 * 2^o (gradient dot products
-// are at most |u| + |v| <= 2 and the trilinear weights are convex), so after
-// octaves 15..o the unsummed rest is at most 2 * (2^o - 1); it is added to the
-// sums' bounds. An undecided level at the end returns false (the exact FP64 path
-// decides). oct(state, o, v) writes octave o of generator state `state`, weight
-// 2^o, for the N levels into v. All 40 octaves go through one loop body with one
-// octave evaluation in it: the unrolled octave code is large, and a body holding
+// summed from the largest octave (weight 2^15) down, stopping once every
+// level's sign is certain, and skipping a sum that no open level of the
+// converged lanes reads (LevelTerms::sel). Octave o contributes at most 2 * 2^o
+// (gradient dot products are at most |u| + |v| <= 2 and the trilinear weights
+// are convex), so after octaves 15..o the unsummed rest is at most
+// 2 * (2^o - 1), which density_sign_lt carries beside the sums' FP32 bounds.
+// An undecided level at the end returns false (the exact FP64 path decides).
+// oct(state, o, v) writes octave o of generator state `state`, weight 2^o, for
+// the N levels into v. All 40 octaves go through one loop body with one octave
+// evaluation in it: the unrolled octave code is large, and a body holding
 // several copies misses the instruction cache on every iteration.
 template <int Y0, int N, typename OctFn>
 __device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsigned& bits) {
@@ -447,11 +455,11 @@ __device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsig
             }
         }
         if (!third) continue;
-        const float err = E_N2_DESC + 2.0f * static_cast<float>((1 << o) - 1);
+        const float rest = 2.0f * static_cast<float>((1 << o) - 1);  // octaves o-1..0, exact in FP32
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             // a closed level keeps its sign: a later interval may straddle 0 again
-            const int sg = density_sign_lt(Y0 + k, lt[k], Fe{a2[k], err}, Fe{a3[k], err});
+            const int sg = density_sign_lt(Y0 + k, lt[k], Fe{a2[k], E_N2_DESC}, Fe{a3[k], E_N2_DESC}, rest);
             const bool was = (open >> k) & 1u;
             pos |= (was && sg > 0) ? 1u << (Y0 + k) : 0u;
             open &= sg != 0 ? ~(1u << k) : ~0u;
