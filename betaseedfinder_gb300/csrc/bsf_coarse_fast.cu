@@ -183,7 +183,7 @@ __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz,
         octave3f<Y0, N>(s.perm + st * PERM_BYTES, ax_x(s, st, kx), ax_z(s, st, kz), s.yf[st],
                         static_cast<float>(1 << o), v, true);
     };
-    return progressive_signs<Y0, N>(Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
+    return progressive_signs<N>(Y0, N, Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
 }
 
 // CT threads per CTA (and columns per tile), MINB CTAs per SM: chosen by the autotuner.

@@ -404,8 +404,8 @@ __device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n
     return (d.v > bound ? 1 : 0) - (d.v < -bound ? 1 : 0);
 }
 
-// Screened signs of one column for levels [Y0, Y0+N) with noise2 and noise3
-// summed from the largest octave (weight 2^15) down, stopping once every
+// Screened signs of one column's levels [y0, y0+n), n <= N, with noise2 and
+// noise3 summed from the largest octave (weight 2^15) down, stopping once every
 // level's sign is certain, and skipping a sum that no open level of the
 // converged lanes reads (LevelTerms::sel). Octave o contributes at most 2 * 2^o
 // (gradient dot products are at most |u| + |v| <= 2 and the trilinear weights
@@ -413,16 +413,17 @@ __device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n
 // 2 * (2^o - 1), which density_sign_lt carries beside the sums' FP32 bounds.
 // An undecided level at the end returns false (the exact FP64 path decides).
 // oct(state, o, v) writes octave o of generator state `state`, weight 2^o, for
-// the N levels into v. All 40 octaves go through one loop body with one octave
-// evaluation in it: the unrolled octave code is large, and a body holding
-// several copies misses the instruction cache on every iteration.
-template <int Y0, int N, typename OctFn>
-__device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsigned& bits) {
+// N levels from y0 into v (a level past n costs its octave work but is never
+// read). All 40 octaves go through one loop body with one octave evaluation in
+// it: the unrolled octave code is large, and a body holding several copies
+// misses the instruction cache on every iteration.
+template <int N, typename OctFn>
+__device__ __forceinline__ bool progressive_signs(int y0, int n, Fe d5, Fe d7, OctFn oct, unsigned& bits) {
     float a1[N], a2[N], a3[N];
     LevelTerms lt[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) a1[k] = a2[k] = a3[k] = 0.0f;  // a skipped sum is read by no open level
-    unsigned open = (1u << N) - 1u, pos = 0;
+    unsigned open = (1u << n) - 1u, pos = 0;
     // steps 0..7: noise1 octaves 0..7 (the reference's order, 0.0 + first term
     // being exact); then for o = 15..0 two steps, noise2 and noise3 octave o
 #pragma unroll 1
@@ -434,7 +435,7 @@ __device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsig
         if (!n1) {
             if (j == 8) {
 #pragma unroll
-                for (int k = 0; k < N; ++k) lt[k] = level_terms(Y0 + k, d5, d7, a1[k]);
+                for (int k = 0; k < N; ++k) lt[k] = level_terms(y0 + k, d5, d7, a1[k]);
             }
             unsigned need = 0;
 #pragma unroll
@@ -459,9 +460,9 @@ __device__ __forceinline__ bool progressive_signs(Fe d5, Fe d7, OctFn oct, unsig
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             // a closed level keeps its sign: a later interval may straddle 0 again
-            const int sg = density_sign_lt(Y0 + k, lt[k], Fe{a2[k], E_N2_DESC}, Fe{a3[k], E_N2_DESC}, rest);
+            const int sg = density_sign_lt(y0 + k, lt[k], Fe{a2[k], E_N2_DESC}, Fe{a3[k], E_N2_DESC}, rest);
             const bool was = (open >> k) & 1u;
-            pos |= (was && sg > 0) ? 1u << (Y0 + k) : 0u;
+            pos |= (was && sg > 0) ? 1u << (y0 + k) : 0u;
             open &= sg != 0 ? ~(1u << k) : ~0u;
         }
         // The converged lanes leave together: a lane that ran ahead into its

@@ -36,7 +36,7 @@ using namespace screen;
 constexpr int NAX = 46;      // distinct coarse coordinates per axis over the 8 centres
 constexpr int NOCT = 66;      // 40 3D + 26 2D lattice octaves (state index == octave index)
 constexpr int PAIR = 2;        // worlds staged per CTA pass (measured: 9% faster than one)
-constexpr int FB_CAP = 512;   // exact-fallback list entries per phase (both worlds)
+constexpr int FB_CAP = 512;   // exact-fallback list entries per round of a phase (both worlds)
 
 __constant__ unsigned char cf_axis[8] = {0, 2, 5, 7, 8, 10, 13, 15};
 __constant__ unsigned char cf_nonaxis_cols[192];
@@ -63,6 +63,8 @@ struct FastSmem {
     std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
     std::uint32_t fb[FB_CAP];             // (range << 13 | slot << 11 | centre << 8 | column)
     int taskCount, fbCount, screened, fallbacks;
+    int fbReserved;                       // fallback entries the claimed chunks may still add
+    int fbLost;                           // set if the list ever overflowed (cannot, see warp_chunks)
     int cursor[3];                        // next unclaimed task of the P20, Upper and Lower phases
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
@@ -97,64 +99,6 @@ __device__ __forceinline__ void column_coords(int c, int col, int& cx, int& cz, 
     kz = iz + center_chunk_z(c) + 15;
 }
 
-// ---- exact FP64 fallback ----------------------------------------------------
-template <int Y0, int N>
-__device__ void exact_octaves(const WorldSmem& s, int base, double sc0, double X, double Z, int count, double* acc) {
-    const GenTable t = gtab(s);
-    double amp = 1.0;
-    for (int o = 0; o < count; ++o) {
-        const Gen g = t(base + o);
-        const double sc = sc0 * amp;
-        YEntry ya[17];
-        exactwarp::y_entries(s, base + o, ya);
-        octave3_column<Y0, N>(g, X * sc, Z * sc, ya, 1.0 / amp, acc, o == 0);
-        amp /= 2.0;
-    }
-}
-
-template <int Y0, int N>
-__device__ unsigned exact_bits(const WorldSmem& s, double X, double Z, double d5, double d7) {
-    double a1[N], a2[N], a3[N];
-    exact_octaves<Y0, N>(s, ST_N2, NOISE_XZ, X, Z, 16, a2);
-    exact_octaves<Y0, N>(s, ST_N3, NOISE_XZ, X, Z, 16, a3);
-    exact_octaves<Y0, N>(s, ST_N1, NOISE_XZ / 80.0, X, Z, 8, a1);
-    unsigned bits = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-        if (density_at(Y0 + k, d5, d7, a1[k], a2[k], a3[k]) > 0.0) bits |= 1u << (Y0 + k);
-    return bits;
-}
-
-// Exact column for Y range id r: 0 -> [11,16) (level 16 is air), 1 -> [0,6), 2 -> [6,11).
-__device__ __noinline__ unsigned exact_task(const WorldSmem& s, int c, int col, int r) {
-    int cx, cz, kx, kz;
-    column_coords(c, col, cx, cz, kx, kz);
-    const GenTable t = gtab(s);
-    double temp, rain, d5, d7;
-    climate_at(t, cx * 4 + 2, cz * 4 + 2, temp, rain);
-    const double X = static_cast<double>(cx), Z = static_cast<double>(cz);
-    double amp = 1.0, acc = 0.0, n4, n5;
-    for (int o = 0; o < 10; ++o) {
-        const double sc = 1.121 * amp;
-        const double v = octave2(t(ST_N4 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n4 = acc;
-    amp = 1.0;
-    for (int o = 0; o < 16; ++o) {
-        const double sc = 200.0 * amp;
-        const double v = octave2(t(ST_N5 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n5 = acc;
-    column_shape(temp, rain, n4, n5, d5, d7);
-    if (r == 0) return exact_bits<11, TOP_SOLID_LEVEL - 10>(s, X, Z, d5, d7);  // level 16: air
-    if (r == 1) return exact_bits<0, 6>(s, X, Z, d5, d7);
-    return exact_bits<6, 5>(s, X, Z, d5, d7);
-}
-
 // ---- screened FP32 path ---------------------------------------------------
 // Column shape (climate + noise4/5); returns false when the d5 branch is undecided.
 __device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, Fe& d5, Fe& d7) {
@@ -177,8 +121,9 @@ __device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, 
     return column_shape_f(temp, rain, Fe{n4, E_N4}, Fe{n5, E_N5}, d5, d7);
 }
 
-// Screened signs of one column for levels [Y0, Y0+N) given its shape; false
-// when undecided.
+// Screened signs of one column's levels [Y0, Y0+N) given its shape; false
+// when undecided. The levels are compile-time: the top fade and the level bits
+// fold into the hot loop.
 template <int Y0, int N>
 __device__ __noinline__ bool screened_range(const WorldSmem& s, int c, int col, Fe d5, Fe d7, unsigned& bits) {
     int cx, cz, kx, kz;
@@ -187,20 +132,30 @@ __device__ __noinline__ bool screened_range(const WorldSmem& s, int c, int col, 
         octave3f<Y0, N>(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz), s.yf[st],
                         static_cast<float>(1 << o), v, true);
     };
-    return progressive_signs<Y0, N>(d5, d7, oct, bits);
+    return progressive_signs<N>(Y0, N, d5, d7, oct, bits);
 }
 
-// A column range the screen left undecided: queued for the exact path, or,
-// when the list is full, given it here.
-__device__ __forceinline__ void fallback_task(FastSmem& s, int q, int c, int col, int r) {
+// Level ranges of the column tasks: 0 -> 11..15 (P20 / Upper; 16 is air),
+// 1 -> 0..5 and 2 -> 6..10 (the Lower groups).
+__device__ __forceinline__ void range_levels(int r, int& y0, int& n) {
+    y0 = r == 0 ? 11 : (r == 1 ? 0 : 6);
+    n = r == 0 ? TOP_SOLID_LEVEL - 10 : (r == 1 ? 6 : 5);
+}
+
+// A column range the screen left undecided, queued for the exact path. The
+// claimed chunks reserved room for it (warp_chunks), so the list cannot be full.
+// Returns 1: the entry the task used.
+__device__ __forceinline__ int fallback_task(FastSmem& s, int q, int c, int col, int r) {
     atomicAdd(&s.fallbacks, 1);
     const int slot = atomicAdd(&s.fbCount, 1);
     if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
-    else atomicOr(&s.w[q].mask17[c][col], exact_task(s.w[q], c, col, r));
+    else s.fbLost = 1;
+    return 1;
 }
 
-// P20 / Upper column task of world slot q: levels 11..15 (16 is air).
-__device__ __forceinline__ void upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+// P20 / Upper column task of world slot q: levels 11..15 (16 is air). Returns
+// the fallback entries it queued (0 or 1).
+__device__ __forceinline__ int upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 1);
     Fe d5, d7;
@@ -208,13 +163,14 @@ __device__ __forceinline__ void upper_task(FastSmem& s, int q, int c, int col, b
     if (!forceExact && screened_shape(w, c, col, d5, d7) &&
         screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, d5, d7, bits)) {
         w.mask17[c][col] = bits;
-        return;
+        return 0;
     }
-    fallback_task(s, q, c, col, 0);
+    return fallback_task(s, q, c, col, 0);
 }
 
 // Lower column task: levels 0..5 and 6..10 (two screened tasks) on one shape.
-__device__ __forceinline__ void lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+// Returns the fallback entries it queued (0 to 2).
+__device__ __forceinline__ int lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 2);
     Fe d5, d7;
@@ -224,48 +180,76 @@ __device__ __forceinline__ void lower_task(FastSmem& s, int q, int c, int col, b
     const bool okHi = shaped && screened_range<6, 5>(w, c, col, d5, d7, hi);
     const unsigned bits = (okLo ? lo : 0u) | (okHi ? hi : 0u);
     if (bits) atomicOr(&w.mask17[c][col], bits);
-    if (!okLo) fallback_task(s, q, c, col, 1);
-    if (!okHi) fallback_task(s, q, c, col, 2);
+    return (okLo ? 0 : fallback_task(s, q, c, col, 1)) + (okHi ? 0 : fallback_task(s, q, c, col, 2));
 }
 
 // Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
 __device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col, int r) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
-    // levels 11..15 (16 is air), 0..5 or 6..10
-    const int y0 = r == 0 ? 11 : (r == 1 ? 0 : 6), n = r == 0 ? TOP_SOLID_LEVEL - 10 : (r == 1 ? 6 : 5);
+    int y0, n;
+    range_levels(r, y0, n);
     return exactwarp::exact_column_warp(s, cx, cz, y0, n);
 }
 
 // A phase's tasks [0, total) handed out 32 at a time to whichever warp asks
 // next: a screened task stops as soon as its signs are certain, so task costs
 // vary, and a fixed split would leave the CTA waiting at the phase's barrier for
-// its slowest warp. Every lane of the warp calls it.
-template <typename F>
-__device__ __forceinline__ void warp_chunks(int* cursor, int total, F body) {
+// its slowest warp. A warp first reserves fallback-list room for the chunk's 32
+// tasks (each adds at most PER entries; body returns how many it did) and hands
+// back what they left unused; it stops claiming when the list could fill, and
+// run_phase then drains the list and hands out the rest. Every lane of the warp
+// calls it.
+template <int PER, typename F>
+__device__ __forceinline__ void warp_chunks(FastSmem& s, int* cursor, int total, F body) {
+    constexpr int RESERVE = 32 * PER;
+    static_assert(RESERVE <= FB_CAP, "one chunk must fit an empty list");
     const int lane = threadIdx.x & 31;
     for (;;) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(cursor, 32);
+        if (lane == 0) {
+            if (atomicAdd(&s.fbReserved, RESERVE) + RESERVE > FB_CAP) {
+                atomicSub(&s.fbReserved, RESERVE);
+                base = -1;
+            } else {
+                base = atomicAdd(cursor, 32);
+                if (base >= total) atomicSub(&s.fbReserved, RESERVE);
+            }
+        }
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= total) break;
-        if (base + lane < total) body(base + lane);
+        if (base < 0 || base >= total) break;
+        const int used = base + lane < total ? body(base + lane) : 0;
+        const int usedAll = __reduce_add_sync(0xffffffffu, used);
+        if (lane == 0) atomicSub(&s.fbReserved, RESERVE - usedAll);
     }
 }
 
-// Fallback pass: one warp per undecided column task.
-__device__ void run_fallbacks(FastSmem& s) {
+// Fallback pass: one warp per undecided column task. Returns whether cursor k
+// still has unclaimed tasks below total, read by every thread between the
+// pass's barriers, before any thread can claim again.
+__device__ bool run_fallbacks(FastSmem& s, int k, int total) {
     __syncthreads();
     const int n = min(s.fbCount, FB_CAP);
-    for (int k = threadIdx.x >> 5; k < n; k += blockDim.x >> 5) {
-        const std::uint32_t e = s.fb[k];
+    for (int f = threadIdx.x >> 5; f < n; f += blockDim.x >> 5) {
+        const std::uint32_t e = s.fb[f];
         const int r = e >> 13, q = (e >> 11) & 1, c = (e >> 8) & 7, col = e & 255;
         const unsigned bits = exact_task_w(s.w[q], c, col, r);
         if ((threadIdx.x & 31) == 0) atomicOr(&s.w[q].mask17[c][col], bits);
     }
     __syncthreads();
-    if (threadIdx.x == 0) s.fbCount = 0;
+    const bool more = s.cursor[k] < total;
+    if (threadIdx.x == 0) s.fbCount = s.fbReserved = 0;
     __syncthreads();
+    return more;
+}
+
+// One phase: screened tasks [0, total) through cursor k, with fallback passes
+// between rounds until every task is claimed.
+template <int PER, typename F>
+__device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body) {
+    do {
+        warp_chunks<PER>(s, &s.cursor[k], total, body);
+    } while (run_fallbacks(s, k, total));
 }
 
 __device__ __forceinline__ int highest_reentry(std::uint32_t mask) {
@@ -291,7 +275,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastSmem& s = *reinterpret_cast<FastSmem*>(smem_raw);
     const int tid = threadIdx.x;
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.fbLost = 0; }
     for (int pair = blockIdx.x; pair * PAIR < n; pair += gridDim.x) {
         const int w0 = pair * PAIR;
         const int nw = min(PAIR, n - w0);
@@ -309,7 +293,10 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             const int c = tid & 7;
             w.p20[c] = 0; w.upper[c] = 0; w.high[c] = 0; w.gate[c] = 0;
         }
-        if (tid == 0) { s.fbCount = 0; s.taskCount = 0; s.cursor[0] = s.cursor[1] = s.cursor[2] = 0; }
+        if (tid == 0) {
+            s.fbCount = s.fbReserved = s.taskCount = 0;
+            s.cursor[0] = s.cursor[1] = s.cursor[2] = 0;
+        }
         for (int k = tid; k < nw * 8 * 256; k += FT) (&s.w[k >> 11].mask17[0][0])[k & 2047] = 0;
         __syncthreads();
         if (tid < OCT3 * nw) {
@@ -336,12 +323,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         const int p20Tasks = centers * 64;
-        warp_chunks(&s.cursor[0], nw * p20Tasks, [&](int t) {
+        run_phase<1>(s, 0, nw * p20Tasks, [&](int t) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
-            upper_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], fs.forceExact);
+            return upper_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], fs.forceExact);
         });
-        run_fallbacks(s);
         for (int t = tid; t < nw * p20Tasks; t += FT) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
@@ -364,11 +350,10 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
         const int upperUnits = s.taskCount;
-        warp_chunks(&s.cursor[1], upperUnits * 192, [&](int t) {
+        run_phase<1>(s, 1, upperUnits * 192, [&](int t) {
             const int e = s.tasks[t / 192];
-            upper_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], fs.forceExact);
+            return upper_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], fs.forceExact);
         });
-        run_fallbacks(s);
         for (int t = tid; t < upperUnits * 192; t += FT) {
             const int e = s.tasks[t / 192];
             if (s.w[e >> 3].mask17[e & 7][cf_nonaxis_cols[t % 192]]) atomicAdd(&s.w[e >> 3].upper[e & 7], 1);
@@ -389,11 +374,10 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239)
         // that share the column's shape.
-        warp_chunks(&s.cursor[2], s.taskCount, [&](int i) {
+        run_phase<2>(s, 2, s.taskCount, [&](int i) {
             const int e = s.tasks[i];
-            lower_task(s, e >> 11, (e >> 8) & 7, e & 255, fs.forceExact);
+            return lower_task(s, e >> 11, (e >> 8) & 7, e & 255, fs.forceExact);
         });
-        run_fallbacks(s);
         // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
         for (int k = tid; k < nw * 8 * 256; k += FT)
             reinterpret_cast<std::uint8_t*>(&s.w[k >> 11].axf[0][0][0])[k & 2047] = 0xFF;
@@ -441,6 +425,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     if (tid == 0 && fs.stats) {
         atomicAdd(&fs.stats[0], static_cast<unsigned long long>(s.screened));
         atomicAdd(&fs.stats[1], static_cast<unsigned long long>(s.fallbacks));
+        if (s.fbLost) atomicAdd(&fs.stats[4], 1ull);
     }
 }
 
