@@ -189,7 +189,7 @@ struct BsfHandle {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stageMs[4] = {0, 0, 0, 0};
     unsigned long long* hPinned = nullptr;  // stage counters [0..7], screen stats [8..11], counters [12..13],
-                                            // coarse retry flag [14], Stage0 fallback-list flag [15]
+                                            // coarse retry flag [14], fallback-list flag [15]
     struct CachedGraph {
         cudaGraphExec_t exec;
         cudaStream_t stream;
@@ -555,7 +555,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
     if (*reinterpret_cast<const int*>(h->hPinned + 14))
         throw std::runtime_error("coarse union-find exceeded its retry bound");
-    if (h->hPinned[15]) throw std::runtime_error("Stage0 fallback list overflowed its reservations");
+    if (h->hPinned[15]) throw std::runtime_error("a screened kernel's fallback list overflowed its reservations");
     read_stage_times(h);
     const auto exactStart = std::chrono::steady_clock::now();
     const int exactN = std::min(hcount[2], h->exactCap);

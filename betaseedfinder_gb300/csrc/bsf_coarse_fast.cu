@@ -26,25 +26,20 @@ constexpr int SIDE = 61;
 constexpr int COLS = SIDE * SIDE;
 constexpr int HALF_ROWS = 31;  // X rows of the first half; the second has 30
 constexpr int NOCT = 66;
-constexpr int MAX_TILE = 512;  // a tile is one column per thread of the CTA
-constexpr int FB_CAP = 256;
-
-struct Y64 {
-    double cellFrac, fade;
-};
+constexpr int HALF_COLS = HALF_ROWS * SIDE;  // columns of the larger half-region
+constexpr int FB_CAP = 512;                   // exact-fallback entries per round
 
 struct CoarseSmem {
     std::uint8_t perm[ST_COUNT * PERM_BYTES];
     double off[ST_COUNT][3];
     YF yf[OCT3][17];
-    Y64 y64[OCT3][17];
     float xf[NOCT][HALF_ROWS], xd[NOCT][HALF_ROWS];
     float zf[NOCT][SIDE], zd[NOCT][SIDE];
     std::uint8_t xi[NOCT][HALF_ROWS], zi[NOCT][SIDE];
-    float shape[MAX_TILE][4];
-    std::uint32_t mask[MAX_TILE];
-    std::uint16_t fb[FB_CAP];
-    int fbCount, screened, fallbacks;
+    float shape[HALF_COLS][4];  // screened column shapes (d5, its bound, d7, its bound; bound < 0: undecided)
+    std::uint32_t mask[HALF_COLS];
+    std::uint16_t fb[FB_CAP];   // (range << 11 | half-local column)
+    int fbCount, fbReserved, cursor, screened, fallbacks, fbLost;
 };
 
 __device__ __forceinline__ GenTable gtab(const CoarseSmem& s) {
@@ -72,39 +67,6 @@ __device__ __forceinline__ AxisF ax_z(const CoarseSmem& s, int o, int k) {
     return AxisF{f, f - 1.0f, s.zd[o][k], s.zi[o][k]};
 }
 
-template <int Y0, int N>
-__device__ void exact_octaves(const CoarseSmem& s, int base, int ycol, double sc0, double X, double Z, int count,
-                              double* acc) {
-    const GenTable t = gtab(s);
-    double amp = 1.0;
-    for (int o = 0; o < count; ++o) {
-        const double sc = sc0 * amp;
-        YEntry ya[17];
-        for (int k = 0; k < N; ++k) {
-            const int y = Y0 + k;
-            ya[y].cellFrac = s.y64[ycol + o][y].cellFrac;
-            ya[y].fade = s.y64[ycol + o][y].fade;
-            ya[y].yi = s.yf[ycol + o][y].yi;
-            ya[y].cell = s.yf[ycol + o][y].cell;
-        }
-        octave3_column<Y0, N>(t(base + o), X * sc, Z * sc, ya, 1.0 / amp, acc, o == 0);
-        amp /= 2.0;
-    }
-}
-
-template <int Y0, int N>
-__device__ unsigned exact_bits(const CoarseSmem& s, double X, double Z, double d5, double d7) {
-    double a1[N], a2[N], a3[N];
-    exact_octaves<Y0, N>(s, ST_N2, 0, NOISE_XZ, X, Z, 16, a2);
-    exact_octaves<Y0, N>(s, ST_N3, 16, NOISE_XZ, X, Z, 16, a3);
-    exact_octaves<Y0, N>(s, ST_N1, 32, NOISE_XZ / 80.0, X, Z, 8, a1);
-    unsigned bits = 0;
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-        if (density_at(Y0 + k, d5, d7, a1[k], a2[k], a3[k]) > 0.0) bits |= 1u << (Y0 + k);
-    return bits;
-}
-
 // Exact FP64 column for Y range r by one whole warp (fallback pass).
 __device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int cz, int r) {
     // level 16 is air
@@ -112,34 +74,6 @@ __device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int
     return exactwarp::exact_column_warp(s, cx, cz, y0, n);
 }
 
-// Exact column in FP64 for Y range r (0: [0,6), 1: [6,12), 2: [12,16), level 16 is air) by one
-// thread: only when the fallback list of a tile overflows.
-__device__ __noinline__ unsigned exact_column(const CoarseSmem& s, int cx, int cz, int r) {
-    const GenTable t = gtab(s);
-    double temp, rain, d5, d7;
-    climate_at(t, cx * 4 + 2, cz * 4 + 2, temp, rain);
-    const double X = static_cast<double>(cx), Z = static_cast<double>(cz);
-    double amp = 1.0, acc = 0.0, n4, n5;
-    for (int o = 0; o < 10; ++o) {
-        const double sc = 1.121 * amp;
-        const double v = octave2(t(ST_N4 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n4 = acc;
-    amp = 1.0;
-    for (int o = 0; o < 16; ++o) {
-        const double sc = 200.0 * amp;
-        const double v = octave2(t(ST_N5 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n5 = acc;
-    column_shape(temp, rain, n4, n5, d5, d7);
-    if (r == 0) return exact_bits<0, 6>(s, X, Z, d5, d7);
-    if (r == 1) return exact_bits<6, 6>(s, X, Z, d5, d7);
-    return exact_bits<12, TOP_SOLID_LEVEL - 11>(s, X, Z, d5, d7);
-}
 
 // Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds; kx is the half-local row.
 // noise5 first: in the d6 < 0 branch d5 is 0.5 whatever the climate and noise4,
@@ -196,7 +130,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
     CoarseSmem& s = *reinterpret_cast<CoarseSmem*>(smem_raw);
     const int tid = threadIdx.x;
     const int jobs = min(*count, maxCount);
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.fbLost = 0; }
     for (int item = blockIdx.x; item < jobs * 2; item += gridDim.x) {
         const int job = item >> 1, half = item & 1;
         const RegionRef ref = queue[job];
@@ -213,7 +147,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             const double* o = cache.offsets + static_cast<std::size_t>(ref.world) * WORLD_OFFSETS;
             for (int k = tid; k < ST_COUNT * 3; k += CT) s.off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
         }
-        if (tid == 0) s.fbCount = 0;
+        if (tid == 0) s.fbCount = s.fbReserved = 0;
         __syncthreads();
         if (tid < OCT3) {
             const int o = tid;
@@ -223,7 +157,6 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             YEntry ya[17];
             build_yaxis(sy, s.off[o][1], ya);
             build_yf(ya, s.yf[o]);
-            for (int y = 0; y < 17; ++y) s.y64[o][y] = Y64{ya[y].cellFrac, ya[y].fade};
         }
         for (int e = tid; e < NOCT * (rows + SIDE); e += CT) {
             const int o = e / (rows + SIDE), k = e % (rows + SIDE);
@@ -241,58 +174,88 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             }
         }
         __syncthreads();
+        // Shapes of the half-region's columns first (kept in smem), then its
+        // 3 x cols column-range tasks handed out 32 at a time: a screened task
+        // stops once its signs are certain, so costs vary, and a fixed split
+        // would leave the CTA waiting for its slowest warp at every barrier.
         const int cols = rows * SIDE;
-        constexpr int TILE = CT;
-        for (int base = 0; base < cols; base += TILE) {
-            const int g = base + tid;  // half-local column: row g / SIDE, z g % SIDE
-            s.mask[tid] = 0;
-            if (g < cols) {
-                const int kx = g / SIDE, kz = g % SIDE;
-                coarse_shape(s, originX + row0 + kx, originZ + kz, kx, kz, s.shape[tid]);
+        for (int g = tid; g < cols; g += CT) {
+            const int kx = g / SIDE, kz = g % SIDE;
+            coarse_shape(s, originX + row0 + kx, originZ + kz, kx, kz, s.shape[g]);
+            s.mask[g] = 0;
+        }
+        if (tid == 0) s.cursor = 0;
+        __syncthreads();
+        // chunk b: range b / chunks of columns (b % chunks) * 32 + lane. Range-major, so
+        // the warps run one range's code at a time (three at once overflow the
+        // instruction cache).
+        const int chunks = (cols + 31) >> 5;
+        const int total = chunks * 3 * 32;
+        auto task = [&](int t) -> int {
+            const int b = t >> 5, r = b / chunks;
+            const int c = (b % chunks) * 32 + (t & 31);
+            if (c >= cols) return 0;
+            const int kx = c / SIDE, kz = c % SIDE;
+            atomicAdd(&s.screened, 1);
+            unsigned bits = 0;
+            bool ok;
+            if (forceExact) ok = false;
+            else if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
+            else if (r == 1) ok = screened_range<6, 6>(s, kx, kz, s.shape[c], bits);
+            else ok = screened_range<12, TOP_SOLID_LEVEL - 11>(s, kx, kz, s.shape[c], bits);  // 16 is air
+            if (ok) {
+                if (bits) atomicOr(&s.mask[c], bits);
+                return 0;
             }
-            __syncthreads();
-            for (int t = tid; t < TILE * 3; t += CT) {
-                const int c = t % TILE, r = t / TILE;
-                const int gg = base + c;
-                if (gg >= cols) continue;
-                const int kx = gg / SIDE, kz = gg % SIDE;
-                atomicAdd(&s.screened, 1);
-                unsigned bits = 0;
-                bool ok;
-                if (forceExact) ok = false;
-                else if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
-                else if (r == 1) ok = screened_range<6, 6>(s, kx, kz, s.shape[c], bits);
-                else ok = screened_range<12, TOP_SOLID_LEVEL - 11>(s, kx, kz, s.shape[c], bits);  // 16 is air
-                if (ok) {
-                    if (bits) atomicOr(&s.mask[c], bits);
-                } else {
-                    atomicAdd(&s.fallbacks, 1);
-                    const int slot = atomicAdd(&s.fbCount, 1);
-                    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint16_t>((r << 12) | c);
-                    else atomicOr(&s.mask[c], exact_column(s, originX + row0 + kx, originZ + kz, r));
+            atomicAdd(&s.fallbacks, 1);
+            const int slot = atomicAdd(&s.fbCount, 1);
+            if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint16_t>((r << 11) | c);
+            else s.fbLost = 1;
+            return 1;
+        };
+        for (;;) {
+            // Claim chunks while the fallback list has room for a whole chunk's
+            // worst case (reserved up front, the unused part handed back).
+            const int lane = tid & 31;
+            for (;;) {
+                int base = 0;
+                if (lane == 0) {
+                    if (atomicAdd(&s.fbReserved, 32) + 32 > FB_CAP) {
+                        atomicSub(&s.fbReserved, 32);
+                        base = -1;
+                    } else {
+                        base = atomicAdd(&s.cursor, 32);
+                        if (base >= total) atomicSub(&s.fbReserved, 32);
+                    }
                 }
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base < 0 || base >= total) break;
+                const int used = __reduce_add_sync(0xffffffffu, base + lane < total ? task(base + lane) : 0);
+                if (lane == 0) atomicSub(&s.fbReserved, 32 - used);
             }
             __syncthreads();
             // fallbacks: one warp per undecided column task
             const int nfb = min(s.fbCount, FB_CAP);
             for (int k = tid >> 5; k < nfb; k += CT >> 5) {
                 const int e = s.fb[k];
-                const int c = e & 0xFFF, r = e >> 12;
-                const int gg = base + c;
-                const unsigned bits = exact_column_w(s, originX + row0 + gg / SIDE, originZ + gg % SIDE, r);
+                const int c = e & 0x7FF, r = e >> 11;
+                const unsigned bits = exact_column_w(s, originX + row0 + c / SIDE, originZ + c % SIDE, r);
                 if ((tid & 31) == 0) atomicOr(&s.mask[c], bits);
             }
             __syncthreads();
-            if (g < cols)
-                signs[static_cast<std::size_t>(job) * COLS + static_cast<std::size_t>(row0) * SIDE + g] = s.mask[tid];
-            if (tid == 0) s.fbCount = 0;
+            const bool more = s.cursor < total;  // read by all before anyone claims again
+            if (tid == 0) s.fbCount = s.fbReserved = 0;
             __syncthreads();
+            if (!more) break;
         }
+        for (int g = tid; g < cols; g += CT)
+            signs[static_cast<std::size_t>(job) * COLS + static_cast<std::size_t>(row0) * SIDE + g] = s.mask[g];
     }
     __syncthreads();
     if (tid == 0 && stats) {
         atomicAdd(&stats[2], static_cast<unsigned long long>(s.screened));
         atomicAdd(&stats[3], static_cast<unsigned long long>(s.fallbacks));
+        if (s.fbLost) atomicAdd(&stats[4], 1ull);
     }
 }
 
