@@ -179,25 +179,46 @@ __device__ __forceinline__ void unite(int* L, int a, int b, int* err) {
     atomicOr(err, 1);
 }
 
+// Initial labels: each run of stone cells along z within a warp's 32 cells
+// points to the run's first cell, which needs no atomics; a row start (z == 0)
+// also starts a run. Planes are (16 nc)^2 = 256 nc^2 cells and the launches use
+// 256-thread blocks, so every warp is full and its cells 32-aligned. Levels
+// below the floor plane are not labelled.
 __global__ void k_cc_init(const std::uint8_t* __restrict__ stone, int* __restrict__ L, int* __restrict__ aux, Dims d) {
     const long long plane = static_cast<long long>(d.SX) * d.SZ;
+    const int lane = threadIdx.x & 31;
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < d.cells;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        L[c] = (c >= plane && stone[c]) ? static_cast<int>(c) : -1;
+        const bool on = c >= plane && stone[c];
+        const int z = static_cast<int>((c % plane) % d.SZ);
+        const unsigned onMask = __ballot_sync(0xffffffffu, on);
+        const bool first = on && (lane == 0 || z == 0 || !((onMask >> (lane - 1)) & 1u));
+        const unsigned starts = __ballot_sync(0xffffffffu, first);
+        const unsigned upTo = starts & (lane == 31 ? 0xffffffffu : ((2u << lane) - 1u));
+        const int runStart = 31 - __clz(upTo);  // on => upTo != 0
+        L[c] = on ? static_cast<int>(c) - (lane - runStart) : -1;
         aux[c] = -1;
     }
 }
 
+// Unions of 6-neighbouring stone cells. Along z only across warp segments
+// (inside one, a run already shares its label); along x and y only where the
+// previous cell of the run did not already link the same two runs (then its
+// union, and the z-links on both sides, connect this pair too).
 __global__ void k_cc_union(const std::uint8_t* __restrict__ stone, int* L, Dims d, int* err) {
     const long long plane = static_cast<long long>(d.SX) * d.SZ;
+    const int lane = threadIdx.x & 31;
     for (long long c = plane + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < d.cells;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         if (!stone[c]) continue;
         const long long rem = c % plane;
         const int x = static_cast<int>(rem / d.SZ), z = static_cast<int>(rem % d.SZ);
-        if (z + 1 < d.SZ && stone[c + 1]) unite(L, static_cast<int>(c), static_cast<int>(c + 1), err);
-        if (x + 1 < d.SX && stone[c + d.SZ]) unite(L, static_cast<int>(c), static_cast<int>(c + d.SZ), err);
-        if (c + plane < d.cells && stone[c + plane]) unite(L, static_cast<int>(c), static_cast<int>(c + plane), err);
+        const bool prev = z > 0 && stone[c - 1];
+        if (lane == 31 && z + 1 < d.SZ && stone[c + 1]) unite(L, static_cast<int>(c), static_cast<int>(c + 1), err);
+        if (x + 1 < d.SX && stone[c + d.SZ] && !(prev && stone[c - 1 + d.SZ]))
+            unite(L, static_cast<int>(c), static_cast<int>(c + d.SZ), err);
+        if (c + plane < d.cells && stone[c + plane] && !(prev && stone[c - 1 + plane]))
+            unite(L, static_cast<int>(c), static_cast<int>(c + plane), err);
     }
 }
 
@@ -271,31 +292,42 @@ __global__ void k_cc_cand(const std::uint8_t* __restrict__ stone, const int* __r
 }
 
 // Per-cell statistics of candidate components (floodFillFlat, :4131-4186).
+// A warp's 32 consecutive cells run along z and mostly share one component, so
+// the lanes are grouped by slot and each group's counts, extremes and flags are
+// reduced in registers; one lane per group updates the slot. (One atomic per
+// cell serialises on the slots of large components.)
 __global__ void k_cc_stats(const std::uint8_t* __restrict__ stone, const int* __restrict__ L,
                            const int* __restrict__ aux, Dims d, SlotStats st) {
     const long long plane = static_cast<long long>(d.SX) * d.SZ;
+    const int lane = threadIdx.x & 31;
     for (long long c = plane + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < d.cells;
          c += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int r = L[c];
-        if (r < 0) continue;
-        const int slot = aux[r];
+        const int slot = r < 0 ? -1 : aux[r];
+        const unsigned group = __match_any_sync(__activemask(), slot);
         if (slot < 0) continue;
         const int ys = static_cast<int>(c / plane);
         const long long rem = c % plane;
         const int x = static_cast<int>(rem / d.SZ), z = static_cast<int>(rem % d.SZ);
         const int wx = d.minWorldX + x, wz = d.minWorldZ + z, y = ys + (FLOOR_Y - 1);
-        atomicAdd(&st.blocks[slot], 1);
-        atomicMin(&st.minX[slot], wx);
-        atomicMax(&st.maxX[slot], wx);
-        atomicMin(&st.minZ[slot], wz);
-        atomicMax(&st.maxZ[slot], wz);
-        atomicMin(&st.minY[slot], y);
-        atomicMax(&st.maxY[slot], y);
         int f = 0;
         if (x == 0 || x == d.SX - 1 || z == 0 || z == d.SZ - 1) f |= FLAG_SIDE;
         // At the flood floor a stone block directly below grounds the component (:4173-4179).
         if (y == FLOOR_Y && stone[c - plane]) f |= FLAG_BOTTOM;
-        if (f) atomicOr(&st.flags[slot], f);
+        const int minX = __reduce_min_sync(group, wx), maxX = __reduce_max_sync(group, wx);
+        const int minZ = __reduce_min_sync(group, wz), maxZ = __reduce_max_sync(group, wz);
+        const int minY = __reduce_min_sync(group, y), maxY = __reduce_max_sync(group, y);
+        const unsigned flags = __reduce_or_sync(group, static_cast<unsigned>(f));
+        if (lane == __ffs(group) - 1) {
+            atomicAdd(&st.blocks[slot], __popc(group));
+            atomicMin(&st.minX[slot], minX);
+            atomicMax(&st.maxX[slot], maxX);
+            atomicMin(&st.minZ[slot], minZ);
+            atomicMax(&st.maxZ[slot], maxZ);
+            atomicMin(&st.minY[slot], minY);
+            atomicMax(&st.maxY[slot], maxY);
+            if (flags) atomicOr(&st.flags[slot], static_cast<int>(flags));
+        }
     }
 }
 
