@@ -265,11 +265,16 @@ def served_form(args, bsf, start):
     chunk = min(B, args.served_chunk)
     n_ranges = args.served_ranges
     blocks = [np.arange(start + i * B, start + (i + 1) * B, dtype=np.int64) for i in range(n_ranges + 1)]
-    pseeds = [int(splitmix(args.seed, 5000 + i) & ((1 << 48) - 1)) for i in range(2 * args.previews + 8)]
+    pseeds = [int(splitmix(args.seed, 5000 + i) & ((1 << 48) - 1)) for i in range(2 * args.previews + 16)]
     with bsf.Server(profile=args.profile, chunk_worlds=chunk, max_lanes=args.served_lanes) as srv:
-        # warm-up: open the lanes the mix will use and capture their batch graphs
-        warm = [srv.submit_range(blocks[n_ranges][: chunk * args.served_lanes])]
-        warm += [srv.submit_preview(pseeds[-1 - i], 0, 0, args.radius) for i in range(4)]
+        # warm-up: one round of the measured pattern (concurrent range requests with
+        # previews arriving between them) on the spare block, so every lane has run
+        # its batch graphs and exact contexts under the same mix before timing
+        wb = blocks[n_ranges]
+        warm = [srv.submit_range(part, radius=args.radius) for part in np.array_split(wb, n_ranges)]
+        for i in range(8):
+            warm.append(srv.submit_preview(pseeds[-1 - i], 0, 0, args.radius))
+            time.sleep(args.preview_interval_ms / 1e3)
         for t in warm:
             srv.wait(t, 120)
             srv.release(t)

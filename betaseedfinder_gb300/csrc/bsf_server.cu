@@ -425,8 +425,16 @@ void* bsf_server_open(const bsf_server_config* cfgIn) {
         S->stopping = true;
         return S;
     }
-    // one resident lane of each class up front, so the first requests find warm state
-    for (int k = 0; k < 2; ++k) {
+    // One resident lane of each class, then the rest of max_lanes range lanes and
+    // preview_lanes preview lanes while they fit the budget, all up front: a lane
+    // opened under load (allocations, graph captures) holds up the requests
+    // already running for about 100 ms. Lanes evicted later reopen on demand.
+    std::vector<int> opening = {BSF_REQ_RANGE, BSF_REQ_PREVIEW};
+    for (int t = 1; t < cfg.max_lanes; ++t) opening.push_back(BSF_REQ_RANGE);
+    for (int t = 1; t < cfg.preview_lanes; ++t) opening.push_back(BSF_REQ_PREVIEW);
+    for (std::size_t i = 0; i < opening.size(); ++i) {
+        const int k = opening[i];
+        if (i >= 2 && S->bytesInUse + S->laneBytes[k] > cfg.hbm_budget_bytes) continue;
         void* h = bsf_open(&S->laneCfg[k]);
         const char* e = h ? bsf_last_error(h) : "handle allocation failed";
         if (!h || (e && e[0])) {
