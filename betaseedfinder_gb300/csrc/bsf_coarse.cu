@@ -254,6 +254,17 @@ __device__ __forceinline__ void unite(int* L, int a, int b, int* err) {
     atomicOr(err, 1);
 }
 
+// First level of the run of set bits of column mask m that holds level y.
+__device__ __forceinline__ int run_start(std::uint32_t m, int y) {
+    const std::uint32_t zerosBelow = ~m & ((1u << y) - 1u);
+    return zerosBelow ? 32 - __clz(zerosBelow) : 0;
+}
+
+// Components are unions of runs: a column's positive cells form at most 9
+// runs along y (contiguous set bits of its 17-bit mask), and a run's cells are
+// 6-connected, so the union-find works on run starts only. Neighbouring runs
+// (z + 1, x + 1) are united once per overlapping pair, and counts, flags and
+// the re-entry test are taken per run. One thread per column throughout.
 __global__ void __launch_bounds__(CC_THREADS) k_coarse_score(const std::uint32_t* __restrict__ signs,
                                                             const RegionRef* __restrict__ queue, const int* count,
                                                             int maxCount, int* __restrict__ labelScratch,
@@ -265,66 +276,99 @@ __global__ void __launch_bounds__(CC_THREADS) k_coarse_score(const std::uint32_t
     int* flg = cnt + COARSE_CELLS;
     __shared__ int best;
     for (int job = blockIdx.x; job < jobs; job += gridDim.x) {
-    const std::uint32_t* sg = signs + static_cast<std::size_t>(job) * COARSE_COLS;
-    __syncthreads();
-    if (threadIdx.x == 0) best = 0;
-    auto pos = [&](int cell) { return (sg[cell / 17] >> (cell % 17)) & 1u; };
-    for (int c = threadIdx.x; c < COARSE_CELLS; c += CC_THREADS) {
-        L[c] = pos(c) ? c : -1;
-        cnt[c] = 0;
-        flg[c] = 0;
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < COARSE_CELLS; c += CC_THREADS) {
-        if (L[c] < 0) continue;
-        const int y = c % 17, col = c / 17, x = col / COARSE_SIDE, z = col % COARSE_SIDE;
-        if (y + 1 < 17 && pos(c + 1)) unite(L, c, c + 1, err);
-        if (z + 1 < COARSE_SIDE && pos(c + 17)) unite(L, c, c + 17, err);
-        if (x + 1 < COARSE_SIDE && pos(c + COARSE_SIDE * 17)) unite(L, c, c + COARSE_SIDE * 17, err);
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < COARSE_CELLS; c += CC_THREADS)
-        if (L[c] >= 0) L[c] = find_root(L, c);
-    __syncthreads();
-    for (int c = threadIdx.x; c < COARSE_CELLS; c += CC_THREADS) {
-        const int r = L[c];
-        if (r < 0) continue;
-        const int y = c % 17, col = c / 17, x = col / COARSE_SIDE, z = col % COARSE_SIDE;
-        atomicAdd(&cnt[r], 1);
-        int f = 0;
-        if (y == 0 || x == 0 || z == 0 || x == COARSE_SIDE - 1 || z == COARSE_SIDE - 1) f |= FLAG_BAD;
-        if (y >= 8) f |= FLAG_TALL;
-        if (f) atomicOr(&flg[r], f);
-    }
-    // Re-entry: the lowest cell of a component in a column with any positive cell below it.
-    for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
-        const std::uint32_t m = sg[col];
-        int seen[9];
-        int nseen = 0;
-        bool below = false;
-        for (int y = 0; y < 17; ++y) {
-            if (!((m >> y) & 1u)) continue;
-            const int r = L[col * 17 + y];
-            bool first = true;
-            for (int k = 0; k < nseen; ++k) first = first && seen[k] != r;
-            if (first) {
-                if (nseen < 9) seen[nseen++] = r;
-                if (below) atomicOr(&flg[r], FLAG_REENTRY);
+        const std::uint32_t* sg = signs + static_cast<std::size_t>(job) * COARSE_COLS;
+        __syncthreads();
+        if (threadIdx.x == 0) best = 0;
+        // run starts are their own roots, with empty statistics
+        for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
+            std::uint32_t m = sg[col];
+            while (m) {
+                const int y = __ffs(m) - 1;
+                const int len = __ffs(~(m >> y)) - 1;
+                const int c = col * 17 + y;
+                L[c] = c;
+                cnt[c] = 0;
+                flg[c] = 0;
+                m &= ~(((1u << len) - 1u) << y);
             }
-            below = true;
         }
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < COARSE_CELLS; c += CC_THREADS) {
-        if (L[c] == c && flg[c] == (FLAG_TALL | FLAG_REENTRY)) atomicMax(&best, cnt[c]);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const RegionRef ref = queue[job];
-        RegionInfo& r = regions[static_cast<std::size_t>(ref.world) * centers + ref.center];
-        r.coarse = best;
-        r.coarseEvaluated = 1;
-    }
+        __syncthreads();
+        for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
+            const std::uint32_t m = sg[col];
+            if (!m) continue;
+            const int x = col / COARSE_SIDE, z = col % COARSE_SIDE;
+            for (int dir = 0; dir < 2; ++dir) {
+                const bool inside = dir == 0 ? z + 1 < COARSE_SIDE : x + 1 < COARSE_SIDE;
+                if (!inside) continue;
+                const int ncol = col + (dir == 0 ? 1 : COARSE_SIDE);
+                const std::uint32_t mn = sg[ncol];
+                const std::uint32_t ov = m & mn;
+                std::uint32_t segs = ov & ~(ov << 1);  // first level of each overlapping stretch
+                while (segs) {
+                    const int y = __ffs(segs) - 1;
+                    unite(L, col * 17 + run_start(m, y), ncol * 17 + run_start(mn, y), err);
+                    segs &= segs - 1;
+                }
+            }
+        }
+        __syncthreads();
+        for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
+            std::uint32_t m = sg[col];
+            while (m) {
+                const int y = __ffs(m) - 1;
+                const int len = __ffs(~(m >> y)) - 1;
+                L[col * 17 + y] = find_root(L, col * 17 + y);
+                m &= ~(((1u << len) - 1u) << y);
+            }
+        }
+        __syncthreads();
+        // per run: its cells, bottom / side contact, height >= 8; and the
+        // re-entry test (IslandSearchEngine's lazy P17 and coarsecore::scoreSigns):
+        // a component's lowest cell in a column with a positive cell below it
+        for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
+            std::uint32_t m = sg[col];
+            const int x = col / COARSE_SIDE, z = col % COARSE_SIDE;
+            const bool side = x == 0 || z == 0 || x == COARSE_SIDE - 1 || z == COARSE_SIDE - 1;
+            int seen[9];
+            int nseen = 0;
+            bool below = false;
+            while (m) {
+                const int y = __ffs(m) - 1;
+                const int len = __ffs(~(m >> y)) - 1;
+                const int r = L[col * 17 + y];
+                atomicAdd(&cnt[r], len);
+                int f = 0;
+                if (y == 0 || side) f |= FLAG_BAD;
+                if (y + len - 1 >= 8) f |= FLAG_TALL;
+                bool first = true;
+                for (int k = 0; k < nseen; ++k) first = first && seen[k] != r;
+                if (first) {
+                    if (nseen < 9) seen[nseen++] = r;
+                    if (below) f |= FLAG_REENTRY;
+                }
+                if (f) atomicOr(&flg[r], f);
+                below = true;
+                m &= ~(((1u << len) - 1u) << y);
+            }
+        }
+        __syncthreads();
+        for (int col = threadIdx.x; col < COARSE_COLS; col += CC_THREADS) {
+            std::uint32_t m = sg[col];
+            while (m) {
+                const int y = __ffs(m) - 1;
+                const int len = __ffs(~(m >> y)) - 1;
+                const int c = col * 17 + y;
+                if (L[c] == c && flg[c] == (FLAG_TALL | FLAG_REENTRY)) atomicMax(&best, cnt[c]);
+                m &= ~(((1u << len) - 1u) << y);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const RegionRef ref = queue[job];
+            RegionInfo& r = regions[static_cast<std::size_t>(ref.world) * centers + ref.center];
+            r.coarse = best;
+            r.coarseEvaluated = 1;
+        }
     }
 }
 

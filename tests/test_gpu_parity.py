@@ -129,3 +129,30 @@ def test_rng_rejection_seeds_match_oracle(worker):
         assert np.array_equal(w.stage0_filter(seeds), po.stage0_batch(seeds, centers=8, profile=1, research=True))
         counts, _ = w.mega_search(seeds)
     assert counts.rng_fallbacks >= len(seeds)   # every one of them took the fallback path
+
+
+def test_mega_pipeline_counts_and_coarse_scores_match_oracle(worker):
+    """The whole queued MEGA pipeline against the oracle's restatement: the stage
+    counts of every gate (P20, Upper, High, P19, Mega, coarse evaluated / passed,
+    islands), every coarse survivor's island, and the coarse score of coarse-
+    evaluated regions, which the 34-byte region records carry."""
+    seeds = consecutive_seeds(1024, 12)
+    counts, recs = worker.mega_search(seeds)
+    rr = worker.last_region_records(len(seeds)).reshape(-1, 34).astype(np.int64)
+    oc, oisl, oreg = po.mega_pipeline(seeds, profile=1, radius=7)
+    got = counts.as_dict()
+    for ours, theirs in (("p20_passed", "p20Passed"), ("upper_passed", "upperPassed"),
+                         ("high_passed", "highPassed"), ("p19_passed", "p19Passed"),
+                         ("mega_rejected", "megaRejected"), ("coarse_evaluated", "coarseEvaluated"),
+                         ("coarse_passed", "coarsePassed"), ("islands", "islands")):
+        assert got[ours] == getattr(oc, theirs), ours
+    ours = sorted((r.world_index * 8 + r.center_index, r.island.key()) for r in recs)
+    assert ours == sorted((int(g), i.key()) for g, i in zip(oreg, oisl))
+    # coarse-evaluated regions: P19 passed and not Mega-rejected
+    evaluated = np.flatnonzero((rr[:, 3] != 0) & (rr[:, 7] == 0))
+    assert len(evaluated) == got["coarse_evaluated"] and len(evaluated) > 0
+    coarse = rr[:, 4] | (rr[:, 5] << 8)
+    for g in evaluated[:24]:
+        w, c = divmod(int(g), 8)
+        assert coarse[g] == min(po.coarse_score(int(seeds[w]), bsf.CENTER_CHUNK_X[c], bsf.CENTER_CHUNK_Z[c]),
+                                65535), (w, c)
