@@ -186,6 +186,16 @@ __host__ __device__ constexpr float octave_sum_bound_desc(int n, float e) {
 }
 constexpr float E_N2_DESC = octave_sum_bound_desc(16, E_OCT3);
 
+// Largest |value| of one legacy 3D octave. The value is the trilinear blend,
+// weights fade(x) fade(y) fade(z) over the 8 cell corners, of gradient terms
+// +-a +- b, where a and b are two distinct components of the corner offset
+// (dx, dy, dz). |dy| < 1 (the legacy cell reuse decouples y's offset from its
+// fade), so a corner's term is at most 1 + max(|dx|, |dz|), and the value is at
+// most F(x, z) = sum over the 4 (x, z) corners of wx wz (1 + max(|dx|, |dz|)).
+// F's maximum over [0, 1]^2 is 1.5353 (on a 2001^2 grid; F is 4.75-Lipschitz
+// in each coordinate, so the true maximum is below 1.538). tests/ recheck it.
+constexpr float OCTAVE3_ABS_MAX = 1.55f;
+
 // Simplex sample with exact FP64 lattice geometry and an FP32 kernel: the
 // offsets d11..d16 are FP64 (they cancel large coordinates), the falloff and
 // gradients are FP32 tracked with bounds. Returns 70*(n0+n1+n2) with its bound.
@@ -407,10 +417,10 @@ __device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n
 // Screened signs of one column's levels [y0, y0+n), n <= N, with noise2 and
 // noise3 summed from the largest octave (weight 2^15) down, stopping once every
 // level's sign is certain, and skipping a sum that no open level of the
-// converged lanes reads (LevelTerms::sel). Octave o contributes at most 2 * 2^o
-// (gradient dot products are at most |u| + |v| <= 2 and the trilinear weights
-// are convex), so after octaves 15..o the unsummed rest is at most
-// 2 * (2^o - 1), which density_sign_lt carries beside the sums' FP32 bounds.
+// converged lanes reads (LevelTerms::sel). Octave o contributes at most
+// OCTAVE3_ABS_MAX * 2^o, so after octaves 15..o the unsummed rest is at most
+// OCTAVE3_ABS_MAX * (2^o - 1), which density_sign_lt carries beside the sums'
+// FP32 bounds.
 // An undecided level at the end returns false (the exact FP64 path decides).
 // oct(state, o, v) writes octave o of generator state `state`, weight 2^o, for
 // N levels from y0 into v (a level past n costs its octave work but is never
@@ -456,7 +466,7 @@ __device__ __forceinline__ bool progressive_signs(int y0, int n, Fe d5, Fe d7, O
             }
         }
         if (!third) continue;
-        const float rest = 2.0f * static_cast<float>((1 << o) - 1);  // octaves o-1..0, exact in FP32
+        const float rest = OCTAVE3_ABS_MAX * static_cast<float>((1 << o) - 1);  // octaves o-1..0
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             // a closed level keeps its sign: a later interval may straddle 0 again
