@@ -74,15 +74,21 @@ struct AxisF {
     int i;
 };
 
+// Axis entry for the FP32 tables: the exact lattice index and fraction of the
+// FP64 coordinate (floor and the subtraction are exact), and the fade rounded
+// to FP32. The fade is evaluated with FMAs, which moves its FP64 value by about
+// 1e-16 before the rounding to FP32 (within the inputs' u|x| model). This runs
+// for every table entry of every staged world, on GB300's narrow FP64 pipe.
 __device__ __forceinline__ AxisF make_axis(double scaled, double offset) {
     double v = scaled + offset;
-    const int fl = jfloor(v);
-    v -= static_cast<double>(fl);
+    const double fl = floor(v);
+    v -= fl;
     AxisF a;
-    a.i = fl & 255;
+    a.i = static_cast<int>(fl) & 255;
     a.f = static_cast<float>(v);
-    a.f1 = static_cast<float>(v - 1.0);
-    a.fd = static_cast<float>(fade(v));
+    a.f1 = a.f - 1.0f;
+    const double t2 = v * v;
+    a.fd = static_cast<float>(t2 * v * fma(v, fma(v, 6.0, -15.0), 10.0));
     return a;
 }
 
