@@ -111,6 +111,9 @@ __device__ __forceinline__ void noise45(const GenTable& t, double X, double Z, d
 // Runs the 4 tasks of the CTA's 64 columns (threads 0..191: 3D Y ranges,
 // 192..255: 2D noise). Column (ix, iz) of the tile sits at coarse
 // (originX + ix, originZ + iz).
+// ABOVE_64: only levels 8..16, which the exact scan's fill reads (blocks at
+// y >= 64); the legacy Y cells still come from the full 17-level tables.
+template <bool ABOVE_64>
 __device__ __forceinline__ void tile_noise(LatticeSmem& s, int originX, int originZ, int side, int tileBase) {
     const int tid = threadIdx.x;
     const int total = side * side;
@@ -120,9 +123,15 @@ __device__ __forceinline__ void tile_noise(LatticeSmem& s, int originX, int orig
         if (g < total) {
             const double X = static_cast<double>(originX + g / side);
             const double Z = static_cast<double>(originZ + g % side);
-            if (grp == 0) lattice_task<0, 6>(s, X, Z, col, s.n1, s.n2, s.n3);
-            else if (grp == 1) lattice_task<6, 6>(s, X, Z, col, s.n1, s.n2, s.n3);
-            else lattice_task<12, 5>(s, X, Z, col, s.n1, s.n2, s.n3);
+            if (ABOVE_64) {
+                if (grp == 0) lattice_task<8, 3>(s, X, Z, col, s.n1, s.n2, s.n3);
+                else if (grp == 1) lattice_task<11, 3>(s, X, Z, col, s.n1, s.n2, s.n3);
+                else lattice_task<14, 3>(s, X, Z, col, s.n1, s.n2, s.n3);
+            } else {
+                if (grp == 0) lattice_task<0, 6>(s, X, Z, col, s.n1, s.n2, s.n3);
+                else if (grp == 1) lattice_task<6, 6>(s, X, Z, col, s.n1, s.n2, s.n3);
+                else lattice_task<12, 5>(s, X, Z, col, s.n1, s.n2, s.n3);
+            }
         }
     } else {
         const int col = tid - 3 * TILE;
@@ -164,7 +173,7 @@ __global__ void __launch_bounds__(256) k_coarse_signs(StateCache cache, const Re
         if (threadIdx.x < TILE) s.mask[threadIdx.x] = 0;
         __syncthreads();
         const int tileBase = tile * TILE;
-        tile_noise(s, originX, originZ, COARSE_SIDE, tileBase);
+        tile_noise<false>(s, originX, originZ, COARSE_SIDE, tileBase);
         if (threadIdx.x >= 3 * TILE) {
             const int col = threadIdx.x - 3 * TILE;
             const int g = tileBase + col;
@@ -188,7 +197,8 @@ __global__ void __launch_bounds__(256) k_coarse_signs(StateCache cache, const Re
     }
 }
 
-// Lattice noise to global memory (exact scan): one job = one lattice.
+// Lattice noise to global memory (exact scan): one job = one lattice, levels
+// 8..16 of n1/n2/n3 (the fill of blocks y >= 64 reads no lower level).
 __global__ void __launch_bounds__(256) k_lattice_noise(StateCache cache, const LatticeJob* __restrict__ jobs,
                                                       LatticeJob single, int side, LatticeBuffers buf) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -203,11 +213,11 @@ __global__ void __launch_bounds__(256) k_lattice_noise(StateCache cache, const L
     build_ytabs(s);
     __syncthreads();
     const int tileBase = tile * TILE;
-    tile_noise(s, J.originX, J.originZ, side, tileBase);
+    tile_noise<true>(s, J.originX, J.originZ, side, tileBase);
     __syncthreads();
     const std::size_t base = static_cast<std::size_t>(job) * buf.columnsPerJob;
-    for (int k = threadIdx.x; k < TILE * 17; k += blockDim.x) {
-        const int col = k / 17, y = k % 17;
+    for (int k = threadIdx.x; k < TILE * 9; k += blockDim.x) {
+        const int col = k / 9, y = 8 + k % 9;  // levels 8..16 only
         const int g = tileBase + col;
         if (g < total) {
             const std::size_t idx = (base + g) * 17 + y;
@@ -422,15 +432,6 @@ void launch_coarse_cc(const RegionRef* dQueue, const int* dCount, int maxCount, 
     k_coarse_score<<<coarse_score_ctas(maxCount), CC_THREADS, 0, stream>>>(
         dSignScratch, dQueue, dCount, maxCount, dLabelScratch, dStatScratch, dRegions, centers, err);
     check(cudaGetLastError(), "k_coarse_score");
-}
-
-void launch_lattice_noise(const StateCache& cache, const LatticeJob* dJobs, int jobs, int side,
-                          const LatticeBuffers& buf, cudaStream_t stream) {
-    if (jobs <= 0) return;
-    ensure_attrs();
-    const int tilesPerJob = (side * side + TILE - 1) / TILE;
-    k_lattice_noise<<<jobs * tilesPerJob, 256, sizeof(LatticeSmem), stream>>>(cache, dJobs, LatticeJob{}, side, buf);
-    check(cudaGetLastError(), "k_lattice_noise");
 }
 
 void launch_lattice_noise_one(const StateCache& cache, const LatticeJob& job, const LatticeBuffers& buf,

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128) k_exact_chunks(StateCache cache, int worl
         climate_at(t, chunkX * 16 + i * 3 + 1, chunkZ * 16 + j * 3 + 1, temp, rain);
         const std::size_t col = static_cast<std::size_t>(a * 4 + i) * d.side + (b * 4 + j);
         column_shape(temp, rain, lat.n4[col], lat.n5[col], d5, d7);
-        for (int y = 0; y < 17; ++y)
+        for (int y = 8; y < 17; ++y)  // the lattice holds levels 8..16: cells 8..15 read no lower level
             s.dens[tid][y] = density_at(y, d5, d7, lat.n1[col * 17 + y], lat.n2[col * 17 + y], lat.n3[col * 17 + y]);
     }
     __syncthreads();

@@ -93,8 +93,7 @@ struct LatticeBuffers {
     double* n5 = nullptr;
     std::size_t columnsPerJob = 0;
 };
-void launch_lattice_noise(const StateCache& cache, const LatticeJob* dJobs, int jobs, int side,
-                          const LatticeBuffers& buf, cudaStream_t stream);
+// Levels 8..16 of n1/n2/n3 and n4/n5 of one exact-scan lattice.
 void launch_lattice_noise_one(const StateCache& cache, const LatticeJob& job, const LatticeBuffers& buf,
                               cudaStream_t stream);
 // Coarse stage for `count` queued regions whose lattices are in `buf` (side 61).
