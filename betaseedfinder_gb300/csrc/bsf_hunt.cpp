@@ -7,10 +7,16 @@
 // reference's record_reject_audits.csv (processLeanRejectAudit,
 // IslandSearchEngine.java:2126-2188; sampling :1403-1476, 2512-2529).
 //
+// It keeps the reference's top-result boards and writes their files
+// (bsf_boards.h).
+//
 //   bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.]
-//                   [capacity=32768] [min_blocks=1000] [audit_mask=0]
+//                   [capacity=32768] [min_blocks=1000] [audit_mask=0] [top_keep=50]
 //   bsf_worker javafmt <value> <precision>      (formatting check: Java's %.<p>f)
+//   bsf_worker boards <top_keep> <outdir>       (board files from records on stdin, one per
+//        line: seed blocks columns centerX centerZ minX maxX minZ maxZ minY maxY radius touches)
 #include "../../include/bsf.h"
+#include "bsf_boards.h"
 
 #include <charconv>
 #include <chrono>
@@ -202,9 +208,12 @@ int hunt_main(int argc, char** argv) {
     const std::int64_t auditMask = argc > 9 ? std::strtoll(argv[9], nullptr, 10) : 0;
     const std::int64_t p20AuditMask =
         (profile == BSF_PROFILE_RECORD60 || profile == BSF_PROFILE_RECORD80) ? auditMask : 32767;
+    const int topKeep = argc > 10 ? std::atoi(argv[10]) : 50;  // SearchSettings.topResultsToKeep
     const Gates gate = gates_of(profile);
-    if (regionsToCheck <= 0 || capacity == 0 || radius < 0 || radius > 24)
-        throw std::invalid_argument("hunt: regions and capacity must be positive and radius 0..24");
+    if (regionsToCheck <= 0 || capacity == 0 || radius < 0 || radius > 24 || topKeep < 1)
+        throw std::invalid_argument("hunt: regions, capacity and top_keep must be positive and radius 0..24");
+    Boards boards(topKeep);
+    boards.write(outdir);  // "No results yet." boards and the CSV header, as at the reference's run start
 
     bsf_config cfg;
     bsf_default_config(&cfg);
@@ -282,6 +291,10 @@ int hunt_main(int argc, char** argv) {
                 else {
                     ++matches;
                     if (r.island.blocks > bestBlocks) bestBlocks = r.island.blocks;
+                    const bsf_island& i = r.island;
+                    boards.add(make_board_record(r.seed, i.blocks, i.columns, i.center_x, i.center_z, i.min_x, i.max_x,
+                                                 i.min_z, i.max_z, i.min_y, i.max_y, i.radius_used,
+                                                 i.touches_side != 0, outdir));
                 }
             }
             const std::int64_t attempt = issuedRegions + regionOffset + 1;
@@ -349,6 +362,7 @@ int hunt_main(int argc, char** argv) {
     }
     std::fclose(csv);
     if (audits) std::fclose(audits);
+    boards.write(outdir);
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     bsf_close(h);
 
@@ -378,6 +392,22 @@ int hunt_main(int argc, char** argv) {
                  static_cast<long long>(regionsToCheck), static_cast<long long>(issuedWorlds),
                  static_cast<long long>(candidates), static_cast<long long>(matches),
                  static_cast<long long>(duplicates), secs);
+    return 0;
+}
+
+int boards_main(int argc, char** argv) {
+    if (argc < 4) throw std::invalid_argument("boards needs <top_keep> <outdir>");
+    const int keep = std::atoi(argv[2]);
+    if (keep < 1) throw std::invalid_argument("boards: top_keep must be positive");
+    const std::string outdir = argv[3];
+    Boards boards(keep);
+    long long seed;
+    int v[12];
+    while (std::scanf("%lld %d %d %d %d %d %d %d %d %d %d %d %d", &seed, &v[0], &v[1], &v[2], &v[3], &v[4], &v[5],
+                      &v[6], &v[7], &v[8], &v[9], &v[10], &v[11]) == 13)
+        boards.add(make_board_record(seed, v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10],
+                                     v[11] != 0, outdir));
+    boards.write(outdir);
     return 0;
 }
 

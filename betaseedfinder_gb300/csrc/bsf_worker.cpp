@@ -227,6 +227,7 @@ int megastream(std::uint32_t capacity, int profile, int radius) {
 namespace bsfhunt {
 int hunt_main(int argc, char** argv);
 int javafmt_main(int argc, char** argv);
+int boards_main(int argc, char** argv);
 }  // namespace bsfhunt
 
 int main(int argc, char** argv) {
@@ -239,12 +240,15 @@ int main(int argc, char** argv) {
                          "  bsf_worker stream [capacity=32768]\n"
                          "  bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]\n"
                          "  bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.] "
-                         "[capacity=32768] [min_blocks=1000]\n");
+                         "[capacity=32768] [min_blocks=1000] [audit_mask=0] [top_keep=50]\n"
+                         "  bsf_worker boards <top_keep> <outdir>   (records on stdin)\n"
+                         "  bsf_worker javafmt <value> <precision>\n");
             return 1;
         }
         const std::string mode = argv[1];
         if (mode == "hunt") return bsfhunt::hunt_main(argc, argv);
         if (mode == "javafmt") return bsfhunt::javafmt_main(argc, argv);
+        if (mode == "boards") return bsfhunt::boards_main(argc, argv);
         const std::uint32_t cap = argc > 2 ? static_cast<std::uint32_t>(std::strtoul(argv[2], nullptr, 10)) : 32768u;
         if (mode == "stream") return p20stream(cap);
         if (mode == "stage0stream") {

@@ -51,6 +51,15 @@ def test_hunt_writes_reference_candidate_rows(tmp_path):
             assert row["status"] in ("no_match", "hot_scan_no_match") and row["finalSource"] == "none"
     manifest = open(os.path.join(tmp_path, "run_manifest.json")).read()
     assert '"seedsToCheck": %d' % regions in manifest and '"worldsChecked": %d' % worlds in manifest
+    # the leaderboard holds the run's unique matches, best first (blocks, columns, area, thickness)
+    unique = [row for row in rows if row["matched"] == "true"]
+    want = sorted(((int(r["verifiedBlocks"]), int(r["columns"]), int(r["footprintArea"]),
+                    int(r["verifiedBlocks"]) / max(1, int(r["columns"])), int(r["seed"])) for r in unique),
+                  key=lambda t: t[:4], reverse=True)[:50]
+    board = [row for row in csv.DictReader(open(os.path.join(tmp_path, "top_island_sideboards.csv")))
+             if row["board"] == "largest"]
+    assert [(int(b["seed"]), int(b["blocks"])) for b in board] == [(t[4], t[0]) for t in want]
+    assert [int(b["rank"]) for b in board] == list(range(1, len(board) + 1))
 
 
 def test_hunt_reject_audits_match_exact_scans(tmp_path):
