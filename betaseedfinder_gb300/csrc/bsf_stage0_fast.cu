@@ -36,7 +36,6 @@ using namespace screen;
 constexpr int NAX = 46;      // distinct coarse coordinates per axis over the 8 centres
 constexpr int NOCT = 66;      // 40 3D + 26 2D lattice octaves (state index == octave index)
 constexpr int PAIR = 2;        // worlds staged per CTA pass (measured: 9% faster than one)
-constexpr int FB_CAP = 512;   // exact-fallback list entries per round of a phase (both worlds)
 
 __constant__ unsigned char cf_axis[8] = {0, 2, 5, 7, 8, 10, 13, 15};
 __constant__ unsigned char cf_nonaxis_cols[192];
@@ -61,10 +60,7 @@ struct alignas(16) WorldSmem {
 struct FastSmem {
     WorldSmem w[PAIR];
     std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
-    std::uint32_t fb[FB_CAP];             // (range << 13 | slot << 11 | centre << 8 | column)
-    int taskCount, fbCount, screened, fallbacks;
-    int fbReserved;                       // fallback entries the claimed chunks may still add
-    int fbLost;                           // set if the list ever overflowed (cannot, see warp_chunks)
+    int taskCount, screened, fallbacks;
     int cursor[3];                        // next unclaimed task of the P20, Upper and Lower phases
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
@@ -142,35 +138,35 @@ __device__ __forceinline__ void range_levels(int r, int& y0, int& n) {
     n = r == 0 ? TOP_SOLID_LEVEL - 10 : (r == 1 ? 6 : 5);
 }
 
-// A column range the screen left undecided, queued for the exact path. The
-// claimed chunks reserved room for it (warp_chunks), so the list cannot be full.
-// Returns 1: the entry the task used.
-__device__ __forceinline__ int fallback_task(FastSmem& s, int q, int c, int col, int r) {
+// Column ranges a task's screen left undecided, for the exact path: up to two
+// entries (range << 13 | slot << 11 | centre << 8 | column), NONE when unused.
+constexpr std::uint32_t NONE = 0xFFFFFFFFu;
+struct Pending {
+    std::uint32_t e[2] = {NONE, NONE};
+};
+__device__ __forceinline__ std::uint32_t fallback_entry(FastSmem& s, int q, int c, int col, int r) {
     atomicAdd(&s.fallbacks, 1);
-    const int slot = atomicAdd(&s.fbCount, 1);
-    if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
-    else s.fbLost = 1;
-    return 1;
+    return static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
 }
 
-// P20 / Upper column task of world slot q: levels 11..15 (16 is air). Returns
-// the fallback entries it queued (0 or 1).
-__device__ __forceinline__ int upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+// P20 / Upper column task of world slot q: levels 11..15 (16 is air).
+__device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 1);
     Fe d5, d7;
     unsigned bits = 0;
+    Pending p;
     if (!forceExact && screened_shape(w, c, col, d5, d7) &&
         screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, d5, d7, bits)) {
         w.mask17[c][col] = bits;
-        return 0;
+        return p;
     }
-    return fallback_task(s, q, c, col, 0);
+    p.e[0] = fallback_entry(s, q, c, col, 0);
+    return p;
 }
 
 // Lower column task: levels 0..5 and 6..10 (two screened tasks) on one shape.
-// Returns the fallback entries it queued (0 to 2).
-__device__ __forceinline__ int lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+__device__ __forceinline__ Pending lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 2);
     Fe d5, d7;
@@ -180,7 +176,10 @@ __device__ __forceinline__ int lower_task(FastSmem& s, int q, int c, int col, bo
     const bool okHi = shaped && screened_range<6, 5>(w, c, col, d5, d7, hi);
     const unsigned bits = (okLo ? lo : 0u) | (okHi ? hi : 0u);
     if (bits) atomicOr(&w.mask17[c][col], bits);
-    return (okLo ? 0 : fallback_task(s, q, c, col, 1)) + (okHi ? 0 : fallback_task(s, q, c, col, 2));
+    Pending p;
+    if (!okLo) p.e[0] = fallback_entry(s, q, c, col, 1);
+    if (!okHi) p.e[1] = fallback_entry(s, q, c, col, 2);
+    return p;
 }
 
 // Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
@@ -195,61 +194,33 @@ __device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col
 // A phase's tasks [0, total) handed out 32 at a time to whichever warp asks
 // next: a screened task stops as soon as its signs are certain, so task costs
 // vary, and a fixed split would leave the CTA waiting at the phase's barrier for
-// its slowest warp. A warp first reserves fallback-list room for the chunk's 32
-// tasks (each adds at most PER entries; body returns how many it did) and hands
-// back what they left unused; it stops claiming when the list could fill, and
-// run_phase then drains the list and hands out the rest. Every lane of the warp
-// calls it.
-template <int PER, typename F>
-__device__ __forceinline__ void warp_chunks(FastSmem& s, int* cursor, int total, F body) {
-    constexpr int RESERVE = 32 * PER;
-    static_assert(RESERVE <= FB_CAP, "one chunk must fit an empty list");
+// its slowest warp. Column ranges the chunk's screen left undecided are
+// resolved right away by the same warp, all 32 lanes on one column
+// (bsf_exact_warp.cuh), while the other warps go on claiming chunks. Every
+// lane of the warp calls it; the phase's barrier follows.
+template <typename F>
+__device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body) {
     const int lane = threadIdx.x & 31;
     for (;;) {
         int base = 0;
-        if (lane == 0) {
-            if (atomicAdd(&s.fbReserved, RESERVE) + RESERVE > FB_CAP) {
-                atomicSub(&s.fbReserved, RESERVE);
-                base = -1;
-            } else {
-                base = atomicAdd(cursor, 32);
-                if (base >= total) atomicSub(&s.fbReserved, RESERVE);
+        if (lane == 0) base = atomicAdd(&s.cursor[k], 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const Pending p = base + lane < total ? body(base + lane) : Pending{};
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            unsigned todo = __ballot_sync(0xffffffffu, p.e[i] != NONE);
+            while (todo) {
+                const int src = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const std::uint32_t e = __shfl_sync(0xffffffffu, p.e[i], src);
+                const int r = e >> 13, q = (e >> 11) & 1, c = (e >> 8) & 7, col = e & 255;
+                const unsigned bits = exact_task_w(s.w[q], c, col, r);
+                if (lane == 0) atomicOr(&s.w[q].mask17[c][col], bits);
             }
         }
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base < 0 || base >= total) break;
-        const int used = base + lane < total ? body(base + lane) : 0;
-        const int usedAll = __reduce_add_sync(0xffffffffu, used);
-        if (lane == 0) atomicSub(&s.fbReserved, RESERVE - usedAll);
-    }
-}
-
-// Fallback pass: one warp per undecided column task. Returns whether cursor k
-// still has unclaimed tasks below total, read by every thread between the
-// pass's barriers, before any thread can claim again.
-__device__ bool run_fallbacks(FastSmem& s, int k, int total) {
-    __syncthreads();
-    const int n = min(s.fbCount, FB_CAP);
-    for (int f = threadIdx.x >> 5; f < n; f += blockDim.x >> 5) {
-        const std::uint32_t e = s.fb[f];
-        const int r = e >> 13, q = (e >> 11) & 1, c = (e >> 8) & 7, col = e & 255;
-        const unsigned bits = exact_task_w(s.w[q], c, col, r);
-        if ((threadIdx.x & 31) == 0) atomicOr(&s.w[q].mask17[c][col], bits);
     }
     __syncthreads();
-    const bool more = s.cursor[k] < total;
-    if (threadIdx.x == 0) s.fbCount = s.fbReserved = 0;
-    __syncthreads();
-    return more;
-}
-
-// One phase: screened tasks [0, total) through cursor k, with fallback passes
-// between rounds until every task is claimed.
-template <int PER, typename F>
-__device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body) {
-    do {
-        warp_chunks<PER>(s, &s.cursor[k], total, body);
-    } while (run_fallbacks(s, k, total));
 }
 
 __device__ __forceinline__ int highest_reentry(std::uint32_t mask) {
@@ -275,7 +246,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastSmem& s = *reinterpret_cast<FastSmem*>(smem_raw);
     const int tid = threadIdx.x;
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.fbLost = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
     for (int pair = blockIdx.x; pair * PAIR < n; pair += gridDim.x) {
         const int w0 = pair * PAIR;
         const int nw = min(PAIR, n - w0);
@@ -294,7 +265,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             w.p20[c] = 0; w.upper[c] = 0; w.high[c] = 0; w.gate[c] = 0;
         }
         if (tid == 0) {
-            s.fbCount = s.fbReserved = s.taskCount = 0;
+            s.taskCount = 0;
             s.cursor[0] = s.cursor[1] = s.cursor[2] = 0;
         }
         for (int k = tid; k < nw * 8 * 256; k += FT) (&s.w[k >> 11].mask17[0][0])[k & 2047] = 0;
@@ -323,7 +294,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         const int p20Tasks = centers * 64;
-        run_phase<1>(s, 0, nw * p20Tasks, [&](int t) {
+        run_phase(s, 0, nw * p20Tasks, [&](int t) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
             return upper_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], fs.forceExact);
@@ -350,7 +321,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
         const int upperUnits = s.taskCount;
-        run_phase<1>(s, 1, upperUnits * 192, [&](int t) {
+        run_phase(s, 1, upperUnits * 192, [&](int t) {
             const int e = s.tasks[t / 192];
             return upper_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], fs.forceExact);
         });
@@ -374,7 +345,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239)
         // that share the column's shape.
-        run_phase<2>(s, 2, s.taskCount, [&](int i) {
+        run_phase(s, 2, s.taskCount, [&](int i) {
             const int e = s.tasks[i];
             return lower_task(s, e >> 11, (e >> 8) & 7, e & 255, fs.forceExact);
         });
@@ -425,7 +396,6 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     if (tid == 0 && fs.stats) {
         atomicAdd(&fs.stats[0], static_cast<unsigned long long>(s.screened));
         atomicAdd(&fs.stats[1], static_cast<unsigned long long>(s.fallbacks));
-        if (s.fbLost) atomicAdd(&fs.stats[4], 1ull);
     }
 }
 
