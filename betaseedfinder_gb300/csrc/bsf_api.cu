@@ -189,7 +189,7 @@ struct BsfHandle {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     float stageMs[4] = {0, 0, 0, 0};
     unsigned long long* hPinned = nullptr;  // stage counters [0..7], screen stats [8..11], counters [12..13],
-                                            // coarse retry flag [14], fallback-list flag [15]
+                                            // coarse retry flag [14]
     struct CachedGraph {
         cudaGraphExec_t exec;
         cudaStream_t stream;
@@ -460,7 +460,7 @@ Island resolve(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, int radiu
 void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seeds) {
     check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
     check(cudaMemsetAsync(h->dStageCounts, 0, 8 * sizeof(unsigned long long), h->stream), "memset");
-    check(cudaMemsetAsync(h->fs.stats, 0, 5 * sizeof(unsigned long long), h->stream), "memset");
+    check(cudaMemsetAsync(h->fs.stats, 0, 4 * sizeof(unsigned long long), h->stream), "memset");
     check(cudaMemsetAsync(h->dCoarseErr, 0, sizeof(int), h->stream), "memset");
     record(h, 0);
     if (seedSource == 2) {
@@ -488,7 +488,6 @@ void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seed
           "counts");
     check(cudaMemcpyAsync(h->hPinned + 14, h->dCoarseErr, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
           "coarse flag");
-    check(cudaMemcpyAsync(h->hPinned + 15, h->fs.stats + 4, 8, cudaMemcpyDeviceToHost, h->stream), "stage0 flag");
 }
 
 // Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters.
@@ -555,7 +554,6 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     if (hcount[0] > h->coarseCap) throw std::runtime_error("coarse queue exceeded its provisioned capacity");
     if (*reinterpret_cast<const int*>(h->hPinned + 14))
         throw std::runtime_error("coarse union-find exceeded its retry bound");
-    if (h->hPinned[15]) throw std::runtime_error("a screened kernel's fallback list overflowed its reservations");
     read_stage_times(h);
     const auto exactStart = std::chrono::steady_clock::now();
     const int exactN = std::min(hcount[2], h->exactCap);

@@ -27,7 +27,6 @@ constexpr int COLS = SIDE * SIDE;
 constexpr int HALF_ROWS = 31;  // X rows of the first half; the second has 30
 constexpr int NOCT = 66;
 constexpr int HALF_COLS = HALF_ROWS * SIDE;  // columns of the larger half-region
-constexpr int FB_CAP = 512;                   // exact-fallback entries per round
 
 struct CoarseSmem {
     std::uint8_t perm[ST_COUNT * PERM_BYTES];
@@ -38,8 +37,7 @@ struct CoarseSmem {
     std::uint8_t xi[NOCT][HALF_ROWS], zi[NOCT][SIDE];
     float shape[HALF_COLS][4];  // screened column shapes (d5, its bound, d7, its bound; bound < 0: undecided)
     std::uint32_t mask[HALF_COLS];
-    std::uint16_t fb[FB_CAP];   // (range << 11 | half-local column)
-    int fbCount, fbReserved, cursor, screened, fallbacks, fbLost;
+    int cursor, screened, fallbacks;
 };
 
 __device__ __forceinline__ GenTable gtab(const CoarseSmem& s) {
@@ -130,7 +128,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
     CoarseSmem& s = *reinterpret_cast<CoarseSmem*>(smem_raw);
     const int tid = threadIdx.x;
     const int jobs = min(*count, maxCount);
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.fbLost = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
     for (int item = blockIdx.x; item < jobs * 2; item += gridDim.x) {
         const int job = item >> 1, half = item & 1;
         const RegionRef ref = queue[job];
@@ -147,7 +145,6 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             const double* o = cache.offsets + static_cast<std::size_t>(ref.world) * WORLD_OFFSETS;
             for (int k = tid; k < ST_COUNT * 3; k += CT) s.off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
         }
-        if (tid == 0) s.fbCount = s.fbReserved = 0;
         __syncthreads();
         if (tid < OCT3) {
             const int o = tid;
@@ -191,10 +188,11 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
         // instruction cache).
         const int chunks = (cols + 31) >> 5;
         const int total = chunks * 3 * 32;
+        // returns the task's column range left undecided (r << 11 | column), or -1
         auto task = [&](int t) -> int {
             const int b = t >> 5, r = b / chunks;
             const int c = (b % chunks) * 32 + (t & 31);
-            if (c >= cols) return 0;
+            if (c >= cols) return -1;
             const int kx = c / SIDE, kz = c % SIDE;
             atomicAdd(&s.screened, 1);
             unsigned bits = 0;
@@ -205,49 +203,31 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             else ok = screened_range<12, TOP_SOLID_LEVEL - 11>(s, kx, kz, s.shape[c], bits);  // 16 is air
             if (ok) {
                 if (bits) atomicOr(&s.mask[c], bits);
-                return 0;
+                return -1;
             }
             atomicAdd(&s.fallbacks, 1);
-            const int slot = atomicAdd(&s.fbCount, 1);
-            if (slot < FB_CAP) s.fb[slot] = static_cast<std::uint16_t>((r << 11) | c);
-            else s.fbLost = 1;
-            return 1;
+            return (r << 11) | c;
         };
+        // Undecided column ranges are resolved right away by the warp that met
+        // them, all 32 lanes on one column, while the other warps go on claiming.
+        const int lane = tid & 31;
         for (;;) {
-            // Claim chunks while the fallback list has room for a whole chunk's
-            // worst case (reserved up front, the unused part handed back).
-            const int lane = tid & 31;
-            for (;;) {
-                int base = 0;
-                if (lane == 0) {
-                    if (atomicAdd(&s.fbReserved, 32) + 32 > FB_CAP) {
-                        atomicSub(&s.fbReserved, 32);
-                        base = -1;
-                    } else {
-                        base = atomicAdd(&s.cursor, 32);
-                        if (base >= total) atomicSub(&s.fbReserved, 32);
-                    }
-                }
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (base < 0 || base >= total) break;
-                const int used = __reduce_add_sync(0xffffffffu, base + lane < total ? task(base + lane) : 0);
-                if (lane == 0) atomicSub(&s.fbReserved, 32 - used);
-            }
-            __syncthreads();
-            // fallbacks: one warp per undecided column task
-            const int nfb = min(s.fbCount, FB_CAP);
-            for (int k = tid >> 5; k < nfb; k += CT >> 5) {
-                const int e = s.fb[k];
-                const int c = e & 0x7FF, r = e >> 11;
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&s.cursor, 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= total) break;
+            const int e = base + lane < total ? task(base + lane) : -1;
+            unsigned todo = __ballot_sync(0xffffffffu, e >= 0);
+            while (todo) {
+                const int src = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int f = __shfl_sync(0xffffffffu, e, src);
+                const int c = f & 0x7FF, r = f >> 11;
                 const unsigned bits = exact_column_w(s, originX + row0 + c / SIDE, originZ + c % SIDE, r);
-                if ((tid & 31) == 0) atomicOr(&s.mask[c], bits);
+                if (lane == 0) atomicOr(&s.mask[c], bits);
             }
-            __syncthreads();
-            const bool more = s.cursor < total;  // read by all before anyone claims again
-            if (tid == 0) s.fbCount = s.fbReserved = 0;
-            __syncthreads();
-            if (!more) break;
         }
+        __syncthreads();
         for (int g = tid; g < cols; g += CT)
             signs[static_cast<std::size_t>(job) * COLS + static_cast<std::size_t>(row0) * SIDE + g] = s.mask[g];
     }
@@ -255,7 +235,6 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
     if (tid == 0 && stats) {
         atomicAdd(&stats[2], static_cast<unsigned long long>(s.screened));
         atomicAdd(&stats[3], static_cast<unsigned long long>(s.fallbacks));
-        if (s.fbLost) atomicAdd(&stats[4], 1ull);
     }
 }
 

@@ -112,8 +112,7 @@ struct Stage0FastScratch {
     int* p19Count = nullptr;
     int p19Capacity = 0;
     unsigned long long* stats = nullptr;  // [0] stage0 column tasks, [1] their FP64 fallbacks,
-                                          // [2] coarse column tasks, [3] their FP64 fallbacks,
-                                          // [4] CTAs whose fallback list overflowed (never: reserved)
+                                          // [2] coarse column tasks, [3] their FP64 fallbacks
     int forceExact = 0;  // verification: treat every screened column task as undecided
 };
 void init_stage0_fast();
