@@ -955,6 +955,160 @@ int or_coarse_score_seed(int64_t seed, int centerChunkX, int centerChunkZ) {
     return s;
 }
 
+/* loadRelevantCoarseGridAroundZero + findBestCoarseFloatingCellsLazy +
+ * hasCoarseReentryColumnForComponent + completeLazyCoarseGridAndScoreFull
+ * (IslandSearchEngine.java:3331-3564, 3726-3759; limits :78-84): component
+ * search from upper-slice starts, lower levels generated per requested column
+ * in rounds, components touching level 0 or the side abandoned at once. The
+ * grid is the coarse lattice of or_coarse_signs (columns through
+ * or_density_column, climate at block 4c+2). */
+int or_coarse_score_lazy_seed(int64_t seed, int centerChunkX, int centerChunkZ, or_lazy_stats* stats) {
+    enum { S = 61, Y = 17, COLS = S * S, CELLS = COLS * Y, MIN_Y = 8 };
+    enum { MAX_LOWER = 512, MAX_ROUNDS = 32, MAX_QUEUE = 12000 };
+    or_world* w = (or_world*)malloc(sizeof(or_world));
+    or_world_init(w, seed);
+    const int fromX = -28 + centerChunkX * 4, fromZ = -28 + centerChunkZ * 4;
+    double* values = (double*)malloc(sizeof(double) * CELLS);
+    uint8_t* lowerDone = (uint8_t*)calloc(COLS, 1);
+    uint8_t* request = (uint8_t*)calloc(COLS, 1);
+    int* labels = (int*)calloc(CELLS, sizeof(int));
+    int* queue = (int*)malloc(sizeof(int) * CELLS);
+    int* colSeen = (int*)calloc(COLS, sizeof(int));
+    int* colMinY = (int*)malloc(sizeof(int) * COLS);
+    int* compCols = (int*)malloc(sizeof(int) * COLS);
+    double col17[17];
+    int lowerColumns = 0, rounds = 0, fallback = 0, best = 0, nextId = 1;
+#define LIDX(x, y, z) (((x) * S + (z)) * Y + (y))
+    for (int i = 0; i < CELLS; ++i) values[i] = -INFINITY;  /* not generated: not positive */
+    for (int x = 0; x < S; ++x)
+        for (int z = 0; z < S; ++z) {
+            const int cx = fromX + x, cz = fromZ + z;
+            or_density_column(w, cx, cz, cx * 4 + 2, cz * 4 + 2, MIN_Y, col17);
+            for (int y = MIN_Y; y < Y; ++y) values[LIDX(x, y, z)] = col17[y];
+        }
+    /* completeCoarseDensityLowerColumnsAroundZeroInto: levels 0..MIN_Y-1 of the requested columns */
+#define COMPLETE_REQUESTED()                                                              \
+    for (int col = 0; col < COLS; ++col) {                                              \
+        if (!request[col] || lowerDone[col]) continue;                                  \
+        const int x = col / S, z = col % S, cx = fromX + x, cz = fromZ + z;               \
+        or_density_column(w, cx, cz, cx * 4 + 2, cz * 4 + 2, 0, col17);                   \
+        for (int y = 0; y < MIN_Y; ++y) values[LIDX(x, y, z)] = col17[y];                  \
+        lowerDone[col] = 1;                                                             \
+        ++lowerColumns;                                                                 \
+    }                                                                                   \
+    memset(request, 0, COLS)
+    for (int x = 0; x < S && !fallback; ++x)
+        for (int z = 0; z < S && !fallback; ++z)
+            for (int y = MIN_Y; y < Y && !fallback; ++y) {
+                const int start = LIDX(x, y, z);
+                if (labels[start] != 0 || !(values[start] > 0.0)) continue;
+                const int id = nextId++;
+                int head = 0, tail = 0, invalid = 0, compRounds = 0;
+                queue[tail++] = start;
+                labels[start] = id;
+                memset(request, 0, COLS);
+                for (;;) {
+                    while (head < tail && !invalid) {
+                        const int idx = queue[head++];
+                        const int cy = idx % Y, tmp = idx / Y, cz = tmp % S, cx = tmp / S;
+                        if (cy == 0 || cx == 0 || cz == 0 || cx == S - 1 || cz == S - 1) {
+                            invalid = 1;
+                            break;
+                        }
+                        static const int dirs[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+                        for (int d = 0; d < 6; ++d) {
+                            const int nx = cx + dirs[d][0], ny = cy + dirs[d][1], nz = cz + dirs[d][2];
+                            if (nx < 0 || nx >= S || ny < 0 || ny >= Y || nz < 0 || nz >= S) continue;
+                            const int ni = LIDX(nx, ny, nz);
+                            if (ny < MIN_Y && !lowerDone[nx * S + nz]) {
+                                request[nx * S + nz] = 1;
+                                continue;
+                            }
+                            if (values[ni] > 0.0) {
+                                if (labels[ni] < 0) {
+                                    invalid = 1;
+                                    break;
+                                }
+                                if (labels[ni] == 0) {
+                                    labels[ni] = id;
+                                    queue[tail++] = ni;
+                                }
+                            }
+                        }
+                    }
+                    if (invalid) break;
+                    int requested = 0;
+                    for (int col = 0; col < COLS; ++col) {
+                        if (request[col] && !lowerDone[col]) ++requested;
+                        else request[col] = 0;
+                    }
+                    if (requested == 0) break;
+                    COMPLETE_REQUESTED();
+                    ++compRounds;
+                    if (lowerColumns > MAX_LOWER || rounds + compRounds > MAX_ROUNDS || tail > MAX_QUEUE) {
+                        fallback = 1;
+                        break;
+                    }
+                    head = 0;  /* new lower cells can neighbour any reached cell: rescan */
+                }
+                if (fallback) break;
+                rounds += compRounds;
+                if (invalid) {
+                    for (int i = 0; i < tail; ++i) labels[queue[i]] = -1;
+                    continue;
+                }
+                int colCount = 0;
+                for (int i = 0; i < tail; ++i) {
+                    const int idx = queue[i];
+                    const int py = idx % Y, col = idx / Y;
+                    if (colSeen[col] != id) {
+                        colSeen[col] = id;
+                        compCols[colCount++] = col;
+                        colMinY[col] = py;
+                    } else if (py < colMinY[col]) {
+                        colMinY[col] = py;
+                    }
+                }
+                if (tail <= best) continue;
+                /* the re-entry test reads the lower slice of every component column */
+                for (int i = 0; i < colCount; ++i)
+                    if (!lowerDone[compCols[i]]) request[compCols[i]] = 1;
+                COMPLETE_REQUESTED();
+                int reentry = 0;
+                for (int i = 0; i < colCount && !reentry; ++i) {
+                    const int col = compCols[i], ccx = col / S, ccz = col % S, minY = colMinY[col];
+                    if (minY <= 0 || minY >= Y) continue;
+                    for (int ly = minY - 1; ly >= 0; --ly) {
+                        const int idx = LIDX(ccx, ly, ccz);
+                        if (values[idx] > 0.0 && labels[idx] != id) {
+                            if (minY - ly - 1 >= 1) reentry = 1;  /* MIN_FLOATING_GAP_STEPS */
+                            break;
+                        }
+                    }
+                }
+                if (reentry) best = tail;
+            }
+    if (fallback) {
+        /* completeLazyCoarseGridAndScoreFull: every lower slice, then the full scorer */
+        for (int col = 0; col < COLS; ++col) request[col] = 1;
+        COMPLETE_REQUESTED();
+        uint8_t* signs = (uint8_t*)malloc(CELLS);
+        for (int i = 0; i < CELLS; ++i) signs[i] = values[i] > 0.0 ? 1 : 0;
+        best = or_coarse_score(signs);
+        free(signs);
+    }
+#undef COMPLETE_REQUESTED
+#undef LIDX
+    if (stats) {
+        stats->lowerColumns = lowerColumns;
+        stats->rounds = rounds;
+        stats->fallbackToFull = fallback;
+    }
+    free(values); free(lowerDone); free(request); free(labels); free(queue);
+    free(colSeen); free(colMinY); free(compCols); free(w);
+    return best;
+}
+
 /* One region through the worker's stage0stream stages
  * (gpu_p20_benchmark.cpp:7421-7502): P20 on the 64 axis columns, Upper on the
  * rest when the gated P20 count is positive, Lower for upper-positive columns

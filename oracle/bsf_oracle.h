@@ -114,6 +114,16 @@ void or_monster_features(const uint8_t* highest256, or_features* f);
 void or_coarse_signs(const or_world* w, int centerChunkX, int centerChunkZ, uint8_t* signs);
 int or_coarse_score(const uint8_t* signs);
 int or_coarse_score_seed(int64_t seed, int centerChunkX, int centerChunkZ);
+
+/* The Java app's component-lazy coarse scorer (P17): the upper slice (levels
+ * 8..16) everywhere, lower levels only for columns a component's search reaches.
+ * A second restatement of the coarse score; it must equal or_coarse_score. */
+typedef struct {
+    int lowerColumns;   /* lower column slices generated */
+    int rounds;         /* expansion rounds */
+    int fallbackToFull; /* a limit was hit and the whole grid was scored */
+} or_lazy_stats;
+int or_coarse_score_lazy_seed(int64_t seed, int centerChunkX, int centerChunkZ, or_lazy_stats* stats);
 void or_coarse_signs_seed(int64_t seed, int centerChunkX, int centerChunkZ, uint8_t* signs);
 
 /* Worker record packing (lean 16 B / research 34 B). */

@@ -82,6 +82,10 @@ class Island(ctypes.Structure):
                 self.minY, self.maxY, self.centerX, self.centerZ, self.touchesSide, self.radiusUsed)
 
 
+class LazyStats(ctypes.Structure):
+    _fields_ = [("lowerColumns", ctypes.c_int32), ("rounds", ctypes.c_int32), ("fallbackToFull", ctypes.c_int32)]
+
+
 class PipelineCounts(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "worlds", "regions", "p20Passed", "upperPassed", "highPassed", "p19Passed",
@@ -109,6 +113,7 @@ def lib():
         L.or_coarse_score_seed.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int]
         L.or_coarse_score.argtypes = [u8p]
         L.or_coarse_signs_seed.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, u8p]
+        L.or_coarse_score_lazy_seed.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int, P(LazyStats)]
         L.or_p19_score.argtypes = [ctypes.c_int, P(Features)]
         L.or_p19_score.restype = ctypes.c_double
         L.or_p19_extreme.argtypes = [P(Features)]
@@ -172,6 +177,13 @@ def coarse_signs(seed, cx=0, cz=0):
 
 def coarse_score(seed, cx=0, cz=0):
     return int(lib().or_coarse_score_seed(seed, cx, cz))
+
+
+def coarse_score_lazy(seed, cx=0, cz=0):
+    """The Java app's component-lazy coarse score (P17) and its generation stats."""
+    st = LazyStats()
+    score = int(lib().or_coarse_score_lazy_seed(seed, cx, cz, ctypes.byref(st)))
+    return score, st
 
 
 def match_settings(**kw):

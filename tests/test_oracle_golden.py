@@ -108,3 +108,29 @@ def test_rejection_seed_states_match_reference():
             h.update(np.asarray(perm, np.uint8).tobytes())
             h.update(np.asarray(abc, np.float64).view(np.uint64).tobytes())
         assert h.hexdigest() == REJECT["ref_states_sha256"][str(sd)], sd
+
+
+def test_lazy_coarse_scorer_agrees_with_the_full_scorer():
+    """The Java app's component-lazy coarse path (P17), restated separately in the
+    oracle, gives the reference's golden scores and the full scorer's score on
+    other seeds and centres, while generating fewer lower column slices."""
+    for rec in GOLDEN["coarse"]:
+        score, st = po.coarse_score_lazy(rec["seed"])
+        assert score == rec["score"], rec
+        assert st.fallbackToFull or st.lowerColumns < 61 * 61
+    rng = np.random.default_rng(17)
+    for _ in range(4):
+        seed = int(rng.integers(-2 ** 62, 2 ** 62))
+        cx, cz = [(0, 0), (15, 0), (-15, 15), (0, -15)][int(rng.integers(0, 4))]
+        assert po.coarse_score_lazy(seed, cx, cz)[0] == po.coarse_score(seed, cx, cz), (seed, cx, cz)
+
+
+def test_coarse_scorers_agree_on_high_scoring_regions():
+    """Regions with large coarse scores (tests/golden/high_coarse_regions.json,
+    made by find_high_coarse_regions.py from the GPU pipeline): the oracle's full
+    scorer and its lazy restatement both give the recorded score."""
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "high_coarse_regions.json")))
+    for r in fx["regions"][:6] + fx["regions"][-2:]:
+        full = po.coarse_score(r["seed"], r["cx"], r["cz"])
+        lazy, _ = po.coarse_score_lazy(r["seed"], r["cx"], r["cz"])
+        assert full == lazy == r["score"], r
