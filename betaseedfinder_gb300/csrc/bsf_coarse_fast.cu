@@ -1,14 +1,17 @@
 // Screened coarse 61x61x17 lattice signs for sm_103a.
 //
-// Persistent grid, two 256-thread CTAs per SM, looping over half-regions
-// (X rows 0..30 and 31..60 of each queued region). Per half-region the CTA
-// stages the world's generators, the 40 3D Y axes (FP32 and FP64) and an axis
-// table of its 31 X and 61 Z coarse coordinates for the 66 lattice octaves
-// (exact FP64 index / fraction / fade, stored as FP32). Columns are processed
-// in tiles of 256: column shape (climate at block 4c+2 + noise4/5), then the
-// three Y ranges of the 40 3D octaves, all in FP32 with error bounds
-// (bsf_screen.cuh). Undecided columns are recomputed in exact FP64, so the
-// 17-bit sign masks equal those of the FP64 coarse kernel bit for bit.
+// Persistent grid of CTAs (launch shape chosen by the autotuner, 512 threads
+// and one CTA per SM on GB300) looping over half-regions (X rows 0..30 and
+// 31..60 of each queued region). Per half-region the CTA stages the world's
+// generators, the 40 FP32 Y axes and an axis table of its 31 X and 61 Z coarse
+// coordinates for the 66 lattice octaves (exact FP64 index / fraction / fade,
+// stored as FP32). It then computes every column's shape (climate at block
+// 4c+2 + noise4/5) into shared memory and hands out the three Y ranges of the
+// columns, 32 tasks at a time, to whichever warp asks next; each task sums the
+// 3D octaves in FP32 with error bounds (bsf_screen.cuh) from the largest down
+// until its signs are certain. Undecided ranges are recomputed in exact FP64 by
+// the warp that met them, so the 17-bit sign masks equal those of the FP64
+// coarse kernel bit for bit.
 #include "bsf_device.cuh"
 #include "bsf_exact_warp.cuh"
 #include "bsf_internal.h"
@@ -118,7 +121,7 @@ __device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz,
     return progressive_signs<N>(Y0, N, Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
 }
 
-// CT threads per CTA (and columns per tile), MINB CTAs per SM: chosen by the autotuner.
+// CT threads per CTA, MINB CTAs per SM: chosen by the autotuner.
 template <int CT, int MINB>
 __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache, const RegionRef* __restrict__ queue,
                                                              const int* count, int maxCount,

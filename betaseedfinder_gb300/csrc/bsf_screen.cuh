@@ -179,7 +179,6 @@ __device__ __forceinline__ float octave2f(const std::uint8_t* p, const AxisF& ax
 __host__ __device__ constexpr float octave_sum_bound(int n, float e) {
     return static_cast<float>((1 << n) - 1) * e + U * 2.0f * static_cast<float>(1 << (n + 1));
 }
-constexpr float E_N2 = octave_sum_bound(16, E_OCT3);  // noise2 / noise3
 constexpr float E_N1 = octave_sum_bound(8, E_OCT3);   // noise1
 constexpr float E_N4 = octave_sum_bound(10, E_OCT2);  // noise4
 constexpr float E_N5 = octave_sum_bound(16, E_OCT2);  // noise5
@@ -490,11 +489,6 @@ __device__ __forceinline__ bool progressive_signs(int y0, int n, Fe d5, Fe d7, O
     return true;
 }
 
-// Density sign at lattice level y from FP32 noise sums with bounds: +1 / -1
-// when decided, 0 when the FP64 value could have either sign.
-__device__ __forceinline__ int density_sign_f(int y, Fe d5, Fe d7, float n1, float n2, float n3) {
-    return density_sign_lt(y, level_terms(y, d5, d7, n1), Fe{n2, E_N2}, Fe{n3, E_N2});
-}
 
 }  // namespace screen
 }  // namespace bsf
