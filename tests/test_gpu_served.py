@@ -91,6 +91,8 @@ def test_served_results_same_alone_and_in_the_mix(workload):
     with bsf.Server(profile="mega", chunk_worlds=4096, max_lanes=1) as s:
         alone_r, alone_p = served_results(s, ranges, previews, interleave=False)
     with bsf.Server(profile="mega", chunk_worlds=4096, max_lanes=4) as s:
+        # every configured lane is open before the first request (the budget allows them all)
+        assert list(s.stats().lanes_open) == [4, 2] and s.stats().evictions == 0
         mix_r, mix_p = served_results(s, ranges, previews, interleave=True)
         st = s.stats()
     assert alone_r == mix_r == direct
