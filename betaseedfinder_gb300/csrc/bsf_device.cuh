@@ -120,6 +120,7 @@ __device__ __forceinline__ void build_yaxis(double sy, double b, YEntry* out) {
     int prev = -1;
     int cell = -1;
     double cellFrac = 0.0;
+#pragma unroll 1
     for (int y = 0; y < 17; ++y) {
         double v = (0.0 + static_cast<double>(y)) * sy + b;
         const int f = jfloor(v);

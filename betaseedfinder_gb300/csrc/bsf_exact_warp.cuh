@@ -25,13 +25,15 @@ __device__ __forceinline__ double lane_value(double v, int src) { return __shfl_
 // The reference's octave accumulation over lanes [first, first + count).
 __device__ __forceinline__ double ordered_sum(double v, int first, int count) {
     double acc = 0.0 + lane_value(v, first);
+#pragma unroll 1
     for (int o = 1; o < count; ++o) acc = acc + lane_value(v, first + o);
     return acc;
 }
 
 // Shape term i of the column: 0..9 the climate simplex octaves (temperature 4,
-// rain 4, blend 2, each with its weight), 10..19 noise4, 20..35 noise5.
-__device__ __forceinline__ double shape_term(const GenTable& t, int i, double X, double Z, double BX, double BZ) {
+// rain 4, blend 2, each with its weight), 10..19 noise4, 20..35 noise5. Out of
+// line, like the steps below, to keep the rarely run fallback code small.
+static __device__ __noinline__ double shape_term(const GenTable& t, int i, double X, double Z, double BX, double BZ) {
     if (i < 10) {
         const int grp = i < 4 ? 0 : (i < 8 ? 1 : 2);
         const int o = i - (grp == 0 ? 0 : (grp == 1 ? 4 : 8));
@@ -98,6 +100,15 @@ __device__ __forceinline__ void octave_terms(const S& s, const GenTable& t, int 
 // are runtime values and every loop has one call site: the path is rare, and
 // unrolled or instantiated per level range its FP64 code (hundreds of KB)
 // streamed through the instruction cache on each call.
+// The fallback path's shape and density steps out of line (code size: the path
+// runs rarely, each time from a cold instruction cache).
+static __device__ __noinline__ void shape_of(double temperature, double rain, double n4, double n5, double& d5, double& d7) {
+    column_shape(temperature, rain, n4, n5, d5, d7);
+}
+static __device__ __noinline__ double density_of(int y, double d5, double d7, double n1, double n2, double n3) {
+    return density_at(y, d5, d7, n1, n2, n3);
+}
+
 template <typename S>
 __device__ unsigned exact_column_warp(const S& s, int cx, int cz, int y0, int n) {
     const int lane = threadIdx.x & 31;
@@ -126,7 +137,7 @@ __device__ unsigned exact_column_warp(const S& s, int cx, int cz, int y0, int n)
     double temperature, rain;
     climate_combine(raw, temperature, rain);
     double d5, d7;
-    column_shape(temperature, rain, n4, n5, d5, d7);
+    shape_of(temperature, rain, n4, n5, d5, d7);
     // 3D octaves: lanes 0-15 noise2, 16-31 noise3, then lanes 0-7 noise1
     double tA[MAX_LEVELS], tB[MAX_LEVELS];
 #pragma unroll 1
@@ -145,7 +156,7 @@ __device__ unsigned exact_column_warp(const S& s, int cx, int cz, int y0, int n)
         const double n2 = ordered_sum(tA[k], 0, 16);
         const double n3 = ordered_sum(tA[k], 16, 16);
         const double n1 = ordered_sum(tB[k], 0, 8);
-        if (density_at(y0 + k, d5, d7, n1, n2, n3) > 0.0) bits |= 1u << (y0 + k);
+        if (density_of(y0 + k, d5, d7, n1, n2, n3) > 0.0) bits |= 1u << (y0 + k);
     }
     return bits;
 }
