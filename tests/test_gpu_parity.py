@@ -156,3 +156,28 @@ def test_mega_pipeline_counts_and_coarse_scores_match_oracle(worker):
         w, c = divmod(int(g), 8)
         assert coarse[g] == min(po.coarse_score(int(seeds[w]), bsf.CENTER_CHUNK_X[c], bsf.CENTER_CHUNK_Z[c]),
                                 65535), (w, c)
+
+
+@pytest.mark.parametrize("profile", ["general", "record60"])
+def test_pipeline_counts_match_oracle_for_other_profiles(profile):
+    """The queued pipeline under the general and record60 gates (P20/Upper/High/
+    coarse thresholds of the worker's hunt profiles) against the oracle's pipeline
+    with the same profile: every stage count and every coarse survivor's island."""
+    seeds = consecutive_seeds(768, 40 + len(profile))
+    with bsf.Worker(capacity=1024, profile=profile, centers=8, max_exact_radius=24) as w:
+        counts, recs = w.mega_search(seeds)
+        rr = w.last_region_records(len(seeds)).reshape(-1, 34).astype(np.int64)
+    oc, oisl, oreg = po.mega_pipeline(seeds, profile=bsf.PROFILES[profile], radius=7)
+    got = counts.as_dict()
+    for ours, theirs in (("p20_passed", "p20Passed"), ("upper_passed", "upperPassed"),
+                         ("high_passed", "highPassed"), ("p19_passed", "p19Passed"),
+                         ("mega_rejected", "megaRejected"), ("coarse_evaluated", "coarseEvaluated"),
+                         ("coarse_passed", "coarsePassed"), ("islands", "islands")):
+        assert got[ours] == getattr(oc, theirs), (profile, ours)
+    assert got["p20_passed"] > 0 and got["coarse_evaluated"] > 0
+    ours = sorted((r.world_index * 8 + r.center_index, r.island.key()) for r in recs)
+    assert ours == sorted((int(g), i.key()) for g, i in zip(oreg, oisl))
+    coarse = rr[:, 4] | (rr[:, 5] << 8)
+    for g in np.flatnonzero((rr[:, 3] != 0) & (rr[:, 7] == 0))[:8]:
+        w_, c = divmod(int(g), 8)
+        assert coarse[g] == po.coarse_score(int(seeds[w_]), bsf.CENTER_CHUNK_X[c], bsf.CENTER_CHUNK_Z[c])
