@@ -550,7 +550,9 @@ def main():
                          "peak": fp32_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                          "traffic": traffic,
                          "peak_source": "measured live: FP32 add issue rate of this GPU (library probe)",
-                         "work_model": "reference-formulation noise ops per lattice column (DESIGN.md)",
+                         "work_model": ("reference-formulation FP64 ops per lattice column: 3D octave 22 + 21/cell + "
+                                        "11/level, 2D octave 37, simplex octave 60, climate and shape 45, "
+                                        "12 per density level"),
                          "fp64_equivalent": {"peak": fp64_peak / 1e12, "frac": achieved / fp64_peak,
                                              "note": "same work against the measured FP64 add rate: "
                                                      "values above 1 are FP64 work avoided by screening"}},
