@@ -63,3 +63,27 @@ def test_random_legacy_octave_values_stay_inside_the_bound():
         value += w * grad3(hashes[:, k], x - cx, cell - cy, z - cz)
     assert (np.abs(value) <= corner_bound(x, z) + 1e-12).all()
     assert np.abs(value).max() <= octave3_abs_max()
+
+
+def test_oracle_legacy_octaves_stay_inside_the_bound():
+    """The oracle's FP64 legacy 3D octave column (17 Y samples with the cell
+    reuse of NoiseGeneratorPerlin173.java:172-285) on real generator states and
+    random lattice coordinates and Y scales: every sample is inside the bound."""
+    import ctypes
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(11)
+    out = np.zeros(17)
+    worst = 0.0
+    for s in range(12):
+        seed = int(rng.integers(-2 ** 62, 2 ** 62))
+        for state in (0, 5, 15, 16, 27, 33, 39):  # noise2, noise3 and noise1 generators
+            perm, abc = po.world_state(seed, state)
+            for _ in range(60):
+                xs, zs = rng.uniform(-5e3, 5e3, 2)
+                sy = float(rng.choice([684.412 / 2 ** k for k in range(16)] + [4.27757 / 2 ** k for k in range(8)]))
+                po.lib().or_perlin_column17_test(perm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                                 abc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                 float(xs), sy, float(zs), 0,
+                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+                worst = max(worst, float(np.abs(out).max()))
+    assert worst <= octave3_abs_max()
