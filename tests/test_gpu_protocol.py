@@ -1,0 +1,55 @@
+"""The drop-in boundary: bsf_worker's stage0stream pipe protocol, as the Java
+scout drives it (GpuStage0Scout.java:143-335; gpu_p20_benchmark.cpp:7310-7502).
+Batches of 1, 3 and the full capacity go in as LE u32 count + LE i64 seeds; the
+answer is the 8-byte magic, then per batch LE u32 count + 34-byte research
+records, each equal to the oracle's. A zero count ends the stream; a batch over
+the capacity and a truncated batch end it with the reference's errors."""
+import struct
+import subprocess
+
+import numpy as np
+import pytest
+
+import betaseedfinder_gb300 as bsf
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+CAPACITY = 64
+
+
+def batch(seeds):
+    return struct.pack("<I", len(seeds)) + b"".join(struct.pack("<q", int(s)) for s in seeds)
+
+
+def test_stage0stream_batches_match_the_oracle():
+    rng = np.random.default_rng(5)
+    batches = [rng.integers(-2 ** 63, 2 ** 63 - 1, size=n, dtype=np.int64) for n in (1, 3, CAPACITY)]
+    stdin = b"".join(batch(b) for b in batches) + struct.pack("<I", 0)
+    r = subprocess.run([bsf.WORKER_PATH, "stage0stream", str(CAPACITY), "mega", "research", "8"], input=stdin,
+                       capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    out = r.stdout
+    assert out[:8] == b"ST0R3816"
+    pos = 8
+    for seeds in batches:
+        (count,) = struct.unpack_from("<I", out, pos)
+        assert count == len(seeds)
+        pos += 4
+        got = np.frombuffer(out, np.uint8, count * 8 * 34, pos)
+        pos += count * 8 * 34
+        want = po.stage0_batch(seeds, centers=8, profile=1, research=True)
+        assert np.array_equal(got, want.reshape(-1))
+    assert pos == len(out)
+
+
+def test_stage0stream_rejects_oversized_and_truncated_batches():
+    seeds = np.arange(CAPACITY + 1, dtype=np.int64)
+    r = subprocess.run([bsf.WORKER_PATH, "stage0stream", str(CAPACITY), "mega", "lean", "8"], input=batch(seeds),
+                       capture_output=True, timeout=300)
+    assert r.returncode == 1
+    assert "Stage0 stream batch exceeds configured world capacity" in r.stderr.decode()
+    truncated = struct.pack("<I", 5) + b"".join(struct.pack("<q", s) for s in (1, 2))
+    r = subprocess.run([bsf.WORKER_PATH, "stage0stream", str(CAPACITY), "mega", "lean", "8"], input=truncated,
+                       capture_output=True, timeout=300)
+    assert r.returncode == 1 and "truncated" in r.stderr.decode()
