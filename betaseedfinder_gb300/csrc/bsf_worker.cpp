@@ -13,7 +13,7 @@
 // on stdin, answered by a LE u32 count and the records. Errors print
 // "ERROR: <message>" on stderr and exit 1; a closed stdout ends cleanly.
 // megastream is the new MEGA mode: same request framing, response = LE u32
-// record count followed by fixed 96-byte island records (see write_mega_record).
+// record count followed by fixed 104-byte island records (see write_mega_record).
 #include "../../include/bsf.h"
 
 #include <cstdint>
@@ -169,9 +169,9 @@ int p20stream(std::uint32_t capacity) {
     return 0;
 }
 
-// 96-byte MEGA record: seed i64, world u32, centre u32, centre chunk x/z i32,
+// 104-byte MEGA record: seed i64, world u32, centre u32, centre chunk x/z i32,
 // p20/upper/high/coarse i32, P19 score f64 bits, island found/blocks/columns,
-// minX/maxX/minZ/maxZ/minY/maxY, centerX/centerZ, touchesSide, radiusUsed i32.
+// minX/maxX/minZ/maxZ/minY/maxY, centerX/centerZ, touchesSide, radiusUsed i32, one zero i32.
 void write_mega_record(std::vector<unsigned char>& o, const bsf_mega_record& r) {
     put_le64(o, static_cast<std::uint64_t>(r.seed));
     put_le32(o, static_cast<std::uint32_t>(r.world_index));

@@ -53,3 +53,33 @@ def test_stage0stream_rejects_oversized_and_truncated_batches():
     r = subprocess.run([bsf.WORKER_PATH, "stage0stream", str(CAPACITY), "mega", "lean", "8"], input=truncated,
                        capture_output=True, timeout=300)
     assert r.returncode == 1 and "truncated" in r.stderr.decode()
+
+
+def test_megastream_records_match_the_api():
+    """megastream: magic, then per batch LE u32 record count + 104-byte records
+    (seed, world, centre, centre chunk x/z, p20, upper, high, coarse, P19 score
+    bits, 14 island ints), equal to the C ABI's MEGA records for the same seeds.
+    The seeds are the fixture's high-coarse regions, so records exist."""
+    import json
+    import os
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "high_coarse_regions.json")))
+    seeds = np.array(sorted({r["seed"] for r in fx["regions"][:8]}), dtype=np.int64)
+    r = subprocess.run([bsf.WORKER_PATH, "megastream", "64", "mega", "7"], input=batch(seeds) + struct.pack("<I", 0),
+                       capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    out = r.stdout
+    assert out[:8] == b"MEGAST01"
+    (n,) = struct.unpack_from("<I", out, 8)
+    assert len(out) == 12 + n * 104 and n > 0
+    with bsf.Worker(capacity=64, profile="mega", centers=8, max_exact_radius=24) as w:
+        _, recs = w.mega_search(seeds, radius=7)
+    assert n == len(recs)
+    for k, rec in enumerate(recs):
+        f = struct.unpack_from("<q8iQ14i", out, 12 + k * 104)
+        assert f[0] == rec.seed
+        assert f[1:9] == (rec.world_index, rec.center_index, rec.center_chunk_x, rec.center_chunk_z, rec.p20,
+                          rec.upper, rec.high, rec.coarse)
+        assert f[9] == struct.unpack("<Q", struct.pack("<d", rec.p19_score))[0]
+        i = rec.island
+        assert f[10:23] == (i.found, i.blocks, i.columns, i.min_x, i.max_x, i.min_z, i.max_z, i.min_y, i.max_y,
+                            i.center_x, i.center_z, i.touches_side, i.radius_used)
