@@ -83,3 +83,24 @@ def test_megastream_records_match_the_api():
         i = rec.island
         assert f[10:23] == (i.found, i.blocks, i.columns, i.min_x, i.max_x, i.min_z, i.max_z, i.min_y, i.max_y,
                             i.center_x, i.center_z, i.touches_side, i.radius_used)
+
+
+def test_p20_stream_bytes_match_the_oracle():
+    """stream (the P20-only fallback path, gpu_p20_benchmark.cpp:7614-7685): magic,
+    then per batch LE u32 count + one clamped P20 count byte per seed."""
+    rng = np.random.default_rng(9)
+    batches = [rng.integers(-2 ** 63, 2 ** 63 - 1, size=n, dtype=np.int64) for n in (2, CAPACITY)]
+    stdin = b"".join(batch(b) for b in batches) + struct.pack("<I", 0)
+    r = subprocess.run([bsf.WORKER_PATH, "stream", str(CAPACITY)], input=stdin, capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr.decode()
+    out = r.stdout
+    assert out[:8] == b"P20STR01"
+    pos = 8
+    for seeds in batches:
+        (count,) = struct.unpack_from("<I", out, pos)
+        assert count == len(seeds)
+        got = np.frombuffer(out, np.uint8, count, pos + 4)
+        pos += 4 + count
+        want = po.stage0_batch(seeds, centers=1, profile=0, research=False).reshape(-1, 16)[:, 0]
+        assert np.array_equal(got, want)
+    assert pos == len(out)
