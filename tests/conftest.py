@@ -1,8 +1,6 @@
 import os
 import sys
 
-import pytest
-
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")  # before any CUDA context (served-mode lanes)
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
