@@ -123,6 +123,12 @@ def test_lazy_coarse_scorer_agrees_with_the_full_scorer():
         seed = int(rng.integers(-2 ** 62, 2 ** 62))
         cx, cz = [(0, 0), (15, 0), (-15, 15), (0, -15)][int(rng.integers(0, 4))]
         assert po.coarse_score_lazy(seed, cx, cz)[0] == po.coarse_score(seed, cx, cz), (seed, cx, cz)
+    # regions whose components pass the lazy limits (512 lower slices, 32 rounds,
+    # 12000 queued cells): the lazy path completes the grid and scores it in full
+    for seed, cx, cz in ((1058, 0, 0), (1059, 0, 15)):
+        score, st = po.coarse_score_lazy(seed, cx, cz)
+        assert st.fallbackToFull and st.lowerColumns == 61 * 61
+        assert score == po.coarse_score(seed, cx, cz), (seed, cx, cz)
 
 
 def test_coarse_scorers_agree_on_high_scoring_regions():
