@@ -121,9 +121,9 @@ def test_per_world_grids_give_identical_results():
 
 
 def test_exact_fallback_paths_alone_match_fp64():
-    """Screening off: every column task goes down the fallback paths (the
-    warp-cooperative FP64 column and, past the fallback list, the per-thread
-    one) and must give the FP64 kernels' records and MEGA results."""
+    """Screening off: every column task goes down the fallback path (the warp
+    resolves each undecided column inline with the warp-cooperative FP64
+    column) and must give the FP64 kernels' records and MEGA results."""
     seeds = consecutive(1024, 888)
     with bsf.Worker(capacity=1024, profile="mega", research=True, centers=8, max_exact_radius=24) as w:
         w.set_mode(bsf.MODE_PLAIN)
