@@ -411,6 +411,32 @@ int boards_main(int argc, char** argv) {
     return 0;
 }
 
+// Candidate-log rows from records given on stdin, one per line: attempt seed p20
+// upper high coarse p19_pass p19_score p19_extreme center_chunk_x center_chunk_z
+// duplicate hot_scanned final_source, then the chosen, raw and hot islands as
+// found blocks columns min_x max_x min_z max_z min_y max_y center_x center_z
+// touches_side radius_used. Writes the header, then one row per record.
+int candrows_main(int, char**) {
+    std::fputs(kHeader, stdout);
+    long long attempt, seed;
+    for (;;) {
+        bsf_mega_record r{};
+        int duplicate = 0;
+        if (std::scanf("%lld %lld %d %d %d %d %d %lf %d %d %d %d %d %d", &attempt, &seed, &r.p20, &r.upper, &r.high,
+                       &r.coarse, &r.p19_pass, &r.p19_score, &r.p19_extreme, &r.center_chunk_x, &r.center_chunk_z,
+                       &duplicate, &r.hot_scanned, &r.final_source) != 14)
+            break;
+        r.seed = seed;
+        for (bsf_island* i : {&r.island, &r.raw_island, &r.hot_island})
+            if (std::scanf("%d %d %d %d %d %d %d %d %d %d %d %d %d", &i->found, &i->blocks, &i->columns, &i->min_x,
+                           &i->max_x, &i->min_z, &i->max_z, &i->min_y, &i->max_y, &i->center_x, &i->center_z,
+                           &i->touches_side, &i->radius_used) != 13)
+                throw std::invalid_argument("candrows: truncated record");
+        std::fputs(candidate_line(attempt, r, duplicate != 0).c_str(), stdout);
+    }
+    return 0;
+}
+
 int javafmt_main(int argc, char** argv) {
     if (argc < 4) throw std::invalid_argument("javafmt needs <value> <precision>");
     std::printf("%s\n", java_fixed(std::strtod(argv[2], nullptr), std::atoi(argv[3])).c_str());

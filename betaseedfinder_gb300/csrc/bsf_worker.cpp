@@ -4,7 +4,11 @@
 //   bsf_worker stream [capacity=32768]
 //   bsf_worker megastream [capacity=32768] [profile=mega] [radius=7]
 //   bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.] [capacity=32768]
-//                   [min_blocks=1000]      (headless search writing hunter_candidates.csv, bsf_hunt.cpp)
+//                   [min_blocks=1000] [audit_mask=0] [top_keep=50]
+//                   (headless search writing hunter_candidates.csv and the result boards, bsf_hunt.cpp)
+//   bsf_worker boards <top_keep> <outdir>   |   bsf_worker candrows   |   bsf_worker javafmt <value> <precision>
+//                   (no GPU: the result boards, candidate-log rows and Java number formatting of
+//                   the hunt's writers, from records given on stdin)
 //
 // stage0stream / stream keep the reference protocol byte for byte
 // (gpu_p20_benchmark.cpp:7310-7685; Java side src/GpuStage0Scout.java:143-335,
@@ -228,6 +232,7 @@ namespace bsfhunt {
 int hunt_main(int argc, char** argv);
 int javafmt_main(int argc, char** argv);
 int boards_main(int argc, char** argv);
+int candrows_main(int argc, char** argv);
 }  // namespace bsfhunt
 
 int main(int argc, char** argv) {
@@ -242,6 +247,7 @@ int main(int argc, char** argv) {
                          "  bsf_worker hunt <sequence_seed> <regions> [profile=mega] [radius=7] [outdir=.] "
                          "[capacity=32768] [min_blocks=1000] [audit_mask=0] [top_keep=50]\n"
                          "  bsf_worker boards <top_keep> <outdir>   (records on stdin)\n"
+                         "  bsf_worker candrows   (records on stdin; candidate-log rows on stdout)\n"
                          "  bsf_worker javafmt <value> <precision>\n");
             return 1;
         }
@@ -249,6 +255,7 @@ int main(int argc, char** argv) {
         if (mode == "hunt") return bsfhunt::hunt_main(argc, argv);
         if (mode == "javafmt") return bsfhunt::javafmt_main(argc, argv);
         if (mode == "boards") return bsfhunt::boards_main(argc, argv);
+        if (mode == "candrows") return bsfhunt::candrows_main(argc, argv);
         const std::uint32_t cap = argc > 2 ? static_cast<std::uint32_t>(std::strtoul(argv[2], nullptr, 10)) : 32768u;
         if (mode == "stream") return p20stream(cap);
         if (mode == "stage0stream") {
