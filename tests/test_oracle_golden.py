@@ -140,3 +140,36 @@ def test_coarse_scorers_agree_on_high_scoring_regions():
         full = po.coarse_score(r["seed"], r["cx"], r["cz"])
         lazy, _ = po.coarse_score_lazy(r["seed"], r["cx"], r["cz"])
         assert full == lazy == r["score"], r
+
+
+STAGE0 = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "stage0_reference.json")))
+
+
+def test_stage0_records_match_reference_sign_grids():
+    """Centre-(0,0) Stage0 records against the values the reference's own coarse
+    sign grids imply (tests/golden/make_stage0_golden.py): P20, Upper and high
+    counts, the twelve P19 features, and the reference's P19 score and extreme
+    flag on them. The general profile's gates (P20 >= 1, Upper >= 5, high >= 5,
+    score >= 4.02) decide which fields the record fills."""
+    regions = STAGE0["regions"]
+    assert sum(r["high"] >= 5 for r in regions) >= 12
+    seeds = np.array([r["seed"] for r in regions], dtype=np.int64)
+    recs = po.stage0_batch(seeds, centers=1, profile=0, research=True).reshape(len(seeds), 34)
+    for r, rec in zip(regions, recs):
+        assert rec[0] == min(r["p20"], 255), r["seed"]
+        upper = min(r["upper"], 255) if r["p20"] >= 1 else 0
+        assert rec[1] == upper, r["seed"]
+        gated = r["p20"] >= 1 and r["upper"] >= 5
+        assert rec[2] == (min(r["high"], 255) if gated else 0), r["seed"]
+        score = rec[8:16].view(np.float64)[0]
+        if gated and r["high"] >= 5:
+            assert format(int(rec[8:16].view(np.uint64)[0]), "016x") == r["p19_score_bits"], r["seed"]
+            f = r["features"]
+            got = [int(rec[16:24].view(np.uint16)[k]) for k in range(4)] + \
+                  [int(rec[24]) | int(rec[25]) << 8, int(rec[26]), int(rec[27]), int(rec[28]),
+                   int(rec[29]) | int(rec[30]) << 8, int(rec[31]), int(rec[32]), int(rec[33])]
+            assert got == f, r["seed"]
+            assert rec[6] == r["p19_extreme"]
+            assert rec[3] == int(r["p19_extreme"] == 1 or score >= 4.02)
+        else:
+            assert np.isnan(score) and rec[3] == 0, r["seed"]
