@@ -69,8 +69,15 @@ def test_stage0_records_research_match_oracle(profile):
 
 
 def test_stage0_single_centre_matches_oracle():
-    seeds = consecutive_seeds(128, 5)
-    with bsf.Worker(capacity=128, profile="general", research=True, centers=1, max_exact_radius=1) as w:
+    """Centre (0,0), general profile, research records. The batch includes the
+    worlds of tests/golden/stage0_reference.json, whose oracle records equal the
+    values the reference's own sign grids imply (test_oracle_golden.py)."""
+    import json
+    import os
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "stage0_reference.json")))
+    pinned = np.array([r["seed"] for r in fx["regions"]], dtype=np.int64)
+    seeds = np.concatenate([consecutive_seeds(128, 5), pinned])
+    with bsf.Worker(capacity=256, profile="general", research=True, centers=1, max_exact_radius=1) as w:
         got = w.stage0_filter(seeds)
     ref = po.stage0_batch(seeds, centers=1, profile=0, research=True)
     assert np.array_equal(got, ref)
