@@ -261,3 +261,81 @@ def ref():
         L.ref_splitmix.restype = ctypes.c_uint64
         _ref = L
     return _ref
+
+
+# ---- the reference worker's own GPU kernels (oracle/ref_gpu.cpp) -------------
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_worker.cubin")
+REF_GPU_LIB = os.path.join(BUILD, "libref_gpu.so")
+
+
+def build_ref_gpu():
+    """Compile the host driver of the reference's GPU kernels (CUDA driver API,
+    linked against the oracle for the host P19 step). Returns the library path,
+    or None when the reference image oracle/_ref/ref_worker.cubin is absent."""
+    if not os.path.exists(REF_CUBIN):
+        return None
+    build()
+    src = os.path.join(HERE, "ref_gpu.cpp")
+    deps = [src, os.path.join(HERE, "bsf_oracle.h"), LIB]
+    if os.path.exists(REF_GPU_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(REF_GPU_LIB) for d in deps):
+        return REF_GPU_LIB
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    tmp = REF_GPU_LIB + ".tmp.%d" % os.getpid()
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-o", tmp, src, "-I" + HERE,
+                           "-I" + os.path.join(cuda, "include"), "-L" + os.path.join(cuda, "lib64", "stubs"),
+                           "-lcuda", "-L" + BUILD, "-loracle", "-Wl,-rpath," + BUILD])
+    os.replace(tmp, REF_GPU_LIB)
+    return REF_GPU_LIB
+
+
+class RefGpu:
+    """The reference worker's stage0stream path on the GPU: its own kernels
+    (compiled unmodified into oracle/_ref/ref_worker.cubin) in its own launch
+    order, with the host steps restated in oracle/ref_gpu.cpp."""
+
+    def __init__(self, capacity, device=0):
+        path = build_ref_gpu()
+        if path is None:
+            raise FileNotFoundError("reference GPU image not built (oracle/_ref/ref_worker.cubin)")
+        L = ctypes.CDLL(path)
+        P = ctypes.POINTER
+        L.rg_open.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+        L.rg_open.restype = ctypes.c_void_p
+        L.rg_stage0_batch.argtypes = [ctypes.c_void_p, P(ctypes.c_int64), ctypes.c_uint32, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, P(ctypes.c_uint8), ctypes.c_char_p,
+                                      ctypes.c_size_t]
+        L.rg_last_ms.argtypes = [ctypes.c_void_p, P(ctypes.c_double)]
+        L.rg_close.argtypes = [ctypes.c_void_p]
+        self.L = L
+        self.capacity = capacity
+        err = ctypes.create_string_buffer(512)
+        self.h = L.rg_open(REF_CUBIN.encode(), device, capacity, err, 512)
+        if not self.h:
+            raise RuntimeError("rg_open: " + err.value.decode())
+
+    def stage0_batch(self, seeds, centers=8, profile=1, research=False):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        rec = 34 if research else 16
+        out = np.zeros(len(seeds) * centers * rec, np.uint8)
+        err = ctypes.create_string_buffer(512)
+        rc = self.L.rg_stage0_batch(self.h, _ptr(seeds, ctypes.c_int64), len(seeds), centers, profile,
+                                    int(research), _ptr(out, ctypes.c_uint8), err, 512)
+        if rc != 0:
+            raise RuntimeError("rg_stage0_batch: " + err.value.decode())
+        return out
+
+    def last_ms(self):
+        ms = np.zeros(3, np.float64)
+        self.L.rg_last_ms(self.h, _ptr(ms, ctypes.c_double))
+        return ms
+
+    def close(self):
+        if self.h:
+            self.L.rg_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
