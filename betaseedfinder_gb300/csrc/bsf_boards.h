@@ -211,10 +211,13 @@ struct Boards {
     explicit Boards(int keep)
         : keep(keep), largest(better_largest, keep), filled(better_filled, keep), raw(better_raw, keep) {}
 
-    void add(const BoardRecord& r) {  // recordTopResult + recordSideboardResults (:4987-5017, 5087-5117)
-        largest.add(r);
+    // recordTopResult + recordSideboardResults (:4987-5017, 5087-5117); true when
+    // the largest board took the record (the reference counts these as topUpdates)
+    bool add(const BoardRecord& r) {
+        const bool top = largest.add(r);
         filled.add(r);
         raw.add(r);
+        return top;
     }
 
     static void write_file(const std::string& path, const std::string& text) {

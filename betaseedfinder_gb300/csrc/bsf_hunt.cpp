@@ -2,7 +2,8 @@
 // (IslandSearchEngine.java:1314-1443, batches of worlds from deterministic
 // seeds, one attempt per region) and its candidate log, hunter_candidates.csv
 // (initializeCandidateCsv / appendCandidateCsv, IslandSearchEngine.java:4826-4960),
-// written from the C ABI's MEGA records, plus a run manifest. With an audit mask
+// written from the C ABI's MEGA records, plus the run manifest (manifest.txt, the
+// reference's key=value format) and the stage counters (run_manifest.json). With an audit mask
 // it also re-scans a sample of rejected regions exactly and logs them like the
 // reference's record_reject_audits.csv (processLeanRejectAudit,
 // IslandSearchEngine.java:2126-2188; sampling :1403-1476, 2512-2529).
@@ -193,6 +194,126 @@ int parse_profile_name(const std::string& v) {
     throw std::invalid_argument("unknown profile " + v);
 }
 
+// Java's Double.toString for the settings written to the manifest: the shortest
+// digits that identify the value, with at least one fractional digit (4.02, 6.7, 2.0).
+std::string java_double(double v) {
+    char buf[64];
+    const auto res = std::to_chars(buf, buf + sizeof(buf), v);
+    std::string t(buf, res.ptr);
+    if (t.find_first_of(".eE") == std::string::npos) t += ".0";
+    return t;
+}
+
+// The settings and outcome of one headless hunt, as manifest.txt records them.
+struct ManifestInfo {
+    std::string status, outdir, label;
+    long long startMs = 0, endMs = 0;
+    std::int64_t checked = 0, matches = 0, topUpdates = 0, regionBudget = 0, sequenceSeed = 0;
+    int profile = BSF_PROFILE_MEGA, radius = 7, topKeep = 50;
+    std::uint32_t capacity = 32768;
+    std::int64_t auditMask = 0;
+    bsf_match_settings ms{};
+};
+
+// writeManifest (IslandSearchEngine.java:4309-4449): "BetaSeedFinder run manifest"
+// then key=value lines in the reference's order and groups, so the app's run
+// history (RunRepository.refresh/parseManifest, RunRepository.java:25-40, 163-171;
+// RunRecord.java:29-41) lists headless hunts beside its own runs. Keys that only
+// describe the app's CPU path or GUI are written with the values a headless GPU
+// hunt has (no previews, no feature log, deterministic seeds).
+void write_manifest(const ManifestInfo& m) {
+    static const char* kProfileName[4] = {"GENERAL", "MEGA 30k+", "RECORD 60k+", "WORLD RECORD 80k+"};
+    const Gates g = gates_of(m.profile);
+    const double p19Min = (m.profile == BSF_PROFILE_RECORD60 || m.profile == BSF_PROFILE_RECORD80) ? 6.70 : 4.02;
+    const bool mega = m.profile == BSF_PROFILE_MEGA;
+    const bool rec60 = m.profile == BSF_PROFILE_RECORD60, rec80 = m.profile == BSF_PROFILE_RECORD80;
+    auto jb = [](bool b) { return b ? "true" : "false"; };
+    std::string s = "BetaSeedFinder run manifest\n";
+    auto kv = [&](const char* k, const std::string& v) { s += std::string(k) + "=" + v + "\n"; };
+    auto ki = [&](const char* k, long long v) { kv(k, std::to_string(v)); };
+    kv("build", "GB300-sm103a-bsf_worker-hunt");
+    kv("status", m.status);
+    kv("runFolder", m.outdir);
+    kv("runLabel", m.label);
+    ki("startEpochMs", m.startMs);
+    ki("endEpochMs", m.endMs);
+    if (m.endMs > m.startMs) {
+        char b[64];
+        std::snprintf(b, sizeof(b), "%.3f", (m.endMs - m.startMs) / 1000.0);
+        kv("elapsedSeconds", b);
+    }
+    ki("checked", m.checked);
+    ki("matches", m.matches);
+    ki("topUpdates", m.topUpdates);
+    kv("checkedUnit", "radius7Regions");
+    ki("regionBudget", m.regionBudget);
+    ki("gpuCoverageCentersPerWorld", 8);
+    ki("gpuCoverageCenterSpacingChunks", 15);
+    kv("gpuProtocol", "ST0R3816");
+    ki("gpuTerrainPerlinCacheStates", 66);
+    ki("gpuClimatePerlinCacheStates", 10);
+    kv("gpuCachedCoarseInitialization", "true");
+    s += "\n";
+    ki("chunkRadius", m.radius);
+    ki("seedsToCheck", m.regionBudget);
+    ki("threads", 1);
+    kv("gpuStage0Enabled", "true");
+    ki("gpuStage0BatchSize", m.capacity);
+    kv("gpuStage0Compatible", "true");
+    kv("gpuStage0Executable", "bsf_worker");
+    kv("gpuP20Enabled", "false");
+    ki("minBlocks", m.ms.min_blocks);
+    ki("minColumns", m.ms.min_columns);
+    ki("minYForMatch", m.ms.min_y_for_match);
+    ki("minWidth", m.ms.min_width);
+    ki("minDepth", m.ms.min_depth);
+    kv("minAvgThickness", java_double(m.ms.min_avg_thickness));
+    ki("topResultsToKeep", m.topKeep);
+    kv("savePreviews", "false");
+    kv("featureLoggingEnabled", "false");
+    kv("filterShadowResearchEnabled", "false");
+    kv("nativeResponseMode", "lean");
+    kv("overnightResearchForcedAuditsEnabled", jb(m.auditMask > 0));
+    s += "\n";
+    kv("hunterMode", "true");
+    ki("huntProfile", m.profile);
+    kv("huntProfileName", kProfileName[m.profile]);
+    kv("megaMode", jb(mega));
+    kv("recordHuntMode", jb(rec60));
+    kv("extremeRecordHuntMode", jb(rec80));
+    ki("effectiveP20MinPositiveColumns", g.p20);
+    kv("effectiveP19MinScore", java_double(p19Min));
+    kv("filterResearchEnabled", "false");
+    ki("megaUpperMinPositiveColumns", g.upper);
+    ki("megaHighMinReentryColumns", g.high);
+    kv("megaExtremeTopologyBypassPreserved", "true");
+    ki("hunterCoarseMinCells", g.coarse);
+    kv("stage075MonsterGateThreshold", java_double(p19Min));
+    kv("stage075MonsterGateTrees", "16");
+    kv("recordRejectAuditPath", m.auditMask > 0 ? m.outdir + "/record_reject_audits.csv" : "");
+    kv("leanTelemetryP19Score", "exactDouble");
+    kv("borderVerifyRadii", "10,13,16,20,24");
+    ki("borderVerifyMaxRadius", 24);
+    ki("dangerousRejectExactScanMinCoarse", g.coarse);
+    kv("hotSeedScanEnabled", "true");
+    ki("hotSeedCoarseThreshold", 120);
+    ki("hotSeedScanRadius", 16);
+    s += "\n";
+    kv("performanceProfilerEnabled", "false");
+    kv("deterministicSeedMode", "true");
+    ki("deterministicSeedSequenceSeed", m.sequenceSeed);
+    const std::string path = m.outdir + "/manifest.txt";
+    std::FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw std::runtime_error("cannot write " + path);
+    std::fwrite(s.data(), 1, s.size(), f);
+    std::fclose(f);
+}
+
+long long epoch_ms() {
+    return std::chrono::duration_cast<std::chrono::milliseconds>(
+               std::chrono::system_clock::now().time_since_epoch()).count();
+}
+
 int hunt_main(int argc, char** argv) {
     if (argc < 4) throw std::invalid_argument("hunt needs <sequence_seed> <regions>");
     const std::int64_t sequenceSeed = std::strtoll(argv[2], nullptr, 10);
@@ -214,6 +335,26 @@ int hunt_main(int argc, char** argv) {
         throw std::invalid_argument("hunt: regions, capacity and top_keep must be positive and radius 0..24");
     Boards boards(topKeep);
     boards.write(outdir);  // "No results yet." boards and the CSV header, as at the reference's run start
+    ManifestInfo mi;
+    {
+        char* abs = realpath(outdir.c_str(), nullptr);
+        mi.outdir = abs ? abs : outdir;
+        std::free(abs);
+        const std::size_t cut = mi.outdir.find_last_of('/');
+        mi.label = cut == std::string::npos ? mi.outdir : mi.outdir.substr(cut + 1);
+    }
+    mi.status = "RUNNING";
+    mi.startMs = epoch_ms();
+    mi.regionBudget = regionsToCheck;
+    mi.sequenceSeed = sequenceSeed;
+    mi.profile = profile;
+    mi.radius = radius;
+    mi.topKeep = topKeep;
+    mi.capacity = capacity;
+    mi.auditMask = auditMask;
+    bsf_default_match_settings(&mi.ms);
+    mi.ms.min_blocks = minBlocks;
+    write_manifest(mi);  // the reference writes a RUNNING manifest at run start (:761)
 
     bsf_config cfg;
     bsf_default_config(&cfg);
@@ -257,6 +398,7 @@ int hunt_main(int argc, char** argv) {
     std::vector<bsf_mega_record> recs(capacity * static_cast<std::size_t>(centers));
     std::set<std::tuple<std::int64_t, int, int, int, int, int, int, int, int>> seen;  // registerUniqueMatch keys
     std::int64_t issuedRegions = 0, issuedWorlds = 0, candidates = 0, matches = 0, duplicates = 0, bestBlocks = 0;
+    std::int64_t topUpdates = 0;
     bsf_stage_counts total{};
     const auto t0 = std::chrono::steady_clock::now();
     while (issuedRegions < regionsToCheck) {
@@ -292,7 +434,7 @@ int hunt_main(int argc, char** argv) {
                     ++matches;
                     if (r.island.blocks > bestBlocks) bestBlocks = r.island.blocks;
                     const bsf_island& i = r.island;
-                    boards.add(make_board_record(r.seed, i.blocks, i.columns, i.center_x, i.center_z, i.min_x, i.max_x,
+                    topUpdates += boards.add(make_board_record(r.seed, i.blocks, i.columns, i.center_x, i.center_z, i.min_x, i.max_x,
                                                  i.min_z, i.max_z, i.min_y, i.max_y, i.radius_used,
                                                  i.touches_side != 0, outdir));
                 }
@@ -365,7 +507,14 @@ int hunt_main(int argc, char** argv) {
     boards.write(outdir);
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     bsf_close(h);
+    mi.status = "FINISHED";
+    mi.endMs = epoch_ms();
+    mi.checked = issuedRegions;
+    mi.matches = matches;
+    mi.topUpdates = topUpdates;
+    write_manifest(mi);
 
+    // the worker's own counters beside the reference manifest (stage counts have no manifest keys)
     const std::string manifestPath = outdir + "/run_manifest.json";
     std::FILE* m = std::fopen(manifestPath.c_str(), "wb");
     if (!m) throw std::runtime_error("cannot write " + manifestPath);

@@ -51,6 +51,24 @@ def test_hunt_writes_reference_candidate_rows(tmp_path):
             assert row["status"] in ("no_match", "hot_scan_no_match") and row["finalSource"] == "none"
     manifest = open(os.path.join(tmp_path, "run_manifest.json")).read()
     assert '"seedsToCheck": %d' % regions in manifest and '"worldsChecked": %d' % worlds in manifest
+    # manifest.txt as the app's run history reads it (RunRepository.parseManifest: split at the first '=',
+    # trim both sides; RunRecord reads build/status/runLabel/epochs/checked/matches/topUpdates)
+    lines = open(os.path.join(tmp_path, "manifest.txt")).read().splitlines()
+    assert lines[0] == "BetaSeedFinder run manifest"
+    kv = {}
+    for line in lines:
+        eq = line.find("=")
+        if eq > 0:
+            kv[line[:eq].strip()] = line[eq + 1:].strip()
+    assert kv["status"] == "FINISHED" and int(kv["checked"]) == regions == int(kv["seedsToCheck"])
+    assert int(kv["matches"]) == sum(1 for row in rows if row["matched"] == "true")
+    assert 0 < int(kv["topUpdates"]) <= int(kv["matches"]) or int(kv["matches"]) == 0
+    assert int(kv["startEpochMs"]) <= int(kv["endEpochMs"]) and float(kv["elapsedSeconds"]) >= 0
+    assert kv["checkedUnit"] == "radius7Regions" and kv["gpuCoverageCentersPerWorld"] == "8"
+    assert kv["huntProfileName"] == "MEGA 30k+" and kv["megaMode"] == "true"
+    assert kv["deterministicSeedMode"] == "true" and int(kv["deterministicSeedSequenceSeed"]) == seq
+    assert kv["chunkRadius"] == "7" and kv["minBlocks"] == "1000" and kv["minAvgThickness"] == "2.0"
+    assert kv["effectiveP19MinScore"] == "4.02" and kv["hunterCoarseMinCells"] == "85"
     # the leaderboard holds the run's unique matches, best first (blocks, columns, area, thickness)
     unique = [row for row in rows if row["matched"] == "true"]
     want = sorted(((int(r["verifiedBlocks"]), int(r["columns"]), int(r["footprintArea"]),
