@@ -514,15 +514,11 @@ static double density_at(int j3, int yLen, double d5, double d7, double n1, doub
 /* BetaTerrain173.generateTerrainNoise (:667-834) over a lattice whose column
  * (i,j) sits at coarse (fromX + i*step, fromZ + j*step); temp/rain hold the
  * climate already sampled for each column (index i*zLen+j). yLen = 17. */
-static void terrain_noise(const or_world* w, double* noise, int fromX, int fromZ, int xLen, int zLen,
-                          int step, const double* temp, const double* rain) {
+/* The five octave sums of generateTerrainNoise (:684-738) over the lattice:
+ * n1/n2/n3 [cols][17], n4/n5 [cols], zero-initialised by the caller. */
+static void terrain_noise_arrays(const or_world* w, int fromX, int fromZ, int xLen, int zLen, int step,
+                                 double* n1, double* n2, double* n3, double* n4, double* n5) {
     const int yLen = 17;
-    int cols = xLen * zLen;
-    double* n4 = (double*)calloc((size_t)cols, sizeof(double));
-    double* n5 = (double*)calloc((size_t)cols, sizeof(double));
-    double* n1 = (double*)calloc((size_t)cols * yLen, sizeof(double));
-    double* n2 = (double*)calloc((size_t)cols * yLen, sizeof(double));
-    double* n3 = (double*)calloc((size_t)cols * yLen, sizeof(double));
     double amp;
     double fx = (double)fromX, fz = (double)fromZ, st = (double)step;
     /* NoiseGeneratorOctaves173.generateNoise (noise/NoiseGeneratorOctaves173.java:46-90). */
@@ -537,6 +533,18 @@ static void terrain_noise(const or_world* w, double* noise, int fromX, int fromZ
     for (int o = 0; o < 16; ++o) { or_perlin_add(&w->n2[o], n2, fx, 0.0, fz, xLen, yLen, zLen, st, st, d0 * amp, d1 * amp, d0 * amp, amp); amp /= 2.0; }
     amp = 1.0;
     for (int o = 0; o < 16; ++o) { or_perlin_add(&w->n3[o], n3, fx, 0.0, fz, xLen, yLen, zLen, st, st, d0 * amp, d1 * amp, d0 * amp, amp); amp /= 2.0; }
+}
+
+static void terrain_noise(const or_world* w, double* noise, int fromX, int fromZ, int xLen, int zLen,
+                          int step, const double* temp, const double* rain) {
+    const int yLen = 17;
+    int cols = xLen * zLen;
+    double* n4 = (double*)calloc((size_t)cols, sizeof(double));
+    double* n5 = (double*)calloc((size_t)cols, sizeof(double));
+    double* n1 = (double*)calloc((size_t)cols * yLen, sizeof(double));
+    double* n2 = (double*)calloc((size_t)cols * yLen, sizeof(double));
+    double* n3 = (double*)calloc((size_t)cols * yLen, sizeof(double));
+    terrain_noise_arrays(w, fromX, fromZ, xLen, zLen, step, n1, n2, n3, n4, n5);
     int k1 = 0;
     for (int c = 0; c < cols; ++c) {
         double d5, d7;
@@ -660,6 +668,22 @@ static uint64_t chunk_bitmap_world(const or_world* w, int chunkX, int chunkZ, ui
     for (int i = 0; i < 32768; ++i)
         if (blocks[i] == 1) bm[i >> 3] |= (uint8_t)(1u << (i & 7));
     return or_bitmap_hash(bm);
+}
+
+/* Test hook: the chunk path's five noise sums at the 5x5 lattice columns of chunk
+ * (chunkX, chunkZ), i.e. coarse (4*chunkX + i, 4*chunkZ + j), column index i*5+j:
+ * n1/n2/n3 [25][17], n4/n5 [25]. */
+void or_chunk_noise_test(int64_t seed, int chunkX, int chunkZ, double* n1, double* n2, double* n3, double* n4,
+                         double* n5) {
+    or_world* w = (or_world*)malloc(sizeof(or_world));
+    or_world_init(w, seed);
+    memset(n1, 0, sizeof(double) * 25 * 17);
+    memset(n2, 0, sizeof(double) * 25 * 17);
+    memset(n3, 0, sizeof(double) * 25 * 17);
+    memset(n4, 0, sizeof(double) * 25);
+    memset(n5, 0, sizeof(double) * 25);
+    terrain_noise_arrays(w, chunkX * 4, chunkZ * 4, 5, 5, 1, n1, n2, n3, n4, n5);
+    free(w);
 }
 
 uint64_t or_chunk_stone_bitmap(int64_t seed, int chunkX, int chunkZ, uint8_t* bm) {

@@ -72,6 +72,10 @@ void or_density_column(const or_world* w, int cx, int cz, int climX, int climZ, 
 void or_chunk_base_terrain(const or_world* w, int chunkX, int chunkZ, uint8_t* blocks);
 /* Stone bitmap: bit (x*16+z)*128+y, LSB first; returns the 64-bit bitmap hash. */
 uint64_t or_chunk_stone_bitmap(int64_t seed, int chunkX, int chunkZ, uint8_t* bitmap4096);
+/* Test hook: the chunk path's noise1..5 sums at the 5x5 lattice columns of a chunk
+ * (coarse (4*chunkX+i, 4*chunkZ+j), index i*5+j); n1..n3 [25][17], n4/n5 [25]. */
+void or_chunk_noise_test(int64_t seed, int chunkX, int chunkZ, double* n1, double* n2, double* n3, double* n4,
+                         double* n5);
 uint64_t or_bitmap_hash(const uint8_t* bitmap4096);
 /* Batch version for tests/baselines: n seeds, optional threads. */
 void or_chunk_bitmaps(const int64_t* seeds, int n, int chunkX, int chunkZ,

@@ -91,6 +91,19 @@ int ref_coarse_score(std::int64_t seed, std::uint8_t* signsOut) {
     return score;
 }
 
+// The reference's coarse noise sums (generateAndScoreHost, coarse_exact_core.hpp:218-386)
+// around centre (0,0): column c = x*61+z at coarse (-28+x, -28+z); n1..n3 [3721][17], n4/n5 [3721].
+void ref_coarse_noise(std::int64_t seed, double* n1, double* n2, double* n3, double* n4, double* n5) {
+    static thread_local coarsecore::HostScratch* scratch = nullptr;
+    if (!scratch) scratch = new coarsecore::HostScratch();
+    coarsecore::generateAndScoreHost(seed, *scratch);
+    std::memcpy(n1, scratch->noise1.data(), sizeof(double) * coarsecore::CELLS);
+    std::memcpy(n2, scratch->noise2.data(), sizeof(double) * coarsecore::CELLS);
+    std::memcpy(n3, scratch->noise3.data(), sizeof(double) * coarsecore::CELLS);
+    std::memcpy(n4, scratch->noise4.data(), sizeof(double) * coarsecore::COLUMNS);
+    std::memcpy(n5, scratch->noise5.data(), sizeof(double) * coarsecore::COLUMNS);
+}
+
 // features[12] = fullY88, fullY96, fullY104, fullY112, y88Largest, y88Width,
 // y88Depth, y88Touches, y96Largest, y96Width, y96Depth, y96Touches
 static p19native::MonsterFeatures to_features(const int* f) {

@@ -89,6 +89,20 @@ def main():
 
     out["splitmix"] = [{"sequence": 123456789, "attempt": a, "seed": str(R.ref_splitmix(123456789, a))}
                        for a in (0, 1, 2, 1000, 2**40)]
+
+    # noise1..5 octave sums of the reference's coarse grid (generateAndScoreHost) at
+    # coarse -28..32 around centre (0,0): the lattice points of the 15x15 chunks of a
+    # radius-7 region, which the chunk path of BetaTerrain173 samples at the same coordinates
+    dp = ctypes.POINTER(ctypes.c_double)
+    R.ref_coarse_noise.argtypes = [ctypes.c_int64] + [dp] * 5
+    chunk_noise = []
+    for seed in [123, -4172144997902289642, 2**48 - 1, 0, 252543233732390] + [int(s) for s in rng.integers(-2**63, 2**63 - 1, 3)]:
+        arrs = [np.zeros(61 * 61 * 17), np.zeros(61 * 61 * 17), np.zeros(61 * 61 * 17), np.zeros(61 * 61),
+                np.zeros(61 * 61)]
+        R.ref_coarse_noise(seed, *[ptr(a, ctypes.c_double) for a in arrs])
+        chunk_noise.append({"seed": seed, "sha256": [hashlib.sha256(a.tobytes()).hexdigest() for a in arrs],
+                            "n2_col0": bits(arrs[1][:17]), "n5_col0": bits(arrs[4][:1])})
+    out["chunk_noise"] = chunk_noise
     with open(OUT, "w") as fh:
         json.dump(out, fh, indent=0, separators=(",", ":"))
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

@@ -62,12 +62,52 @@ def test_coarse_signs_and_scores_match_reference():
         assert po.coarse_score(rec["seed"]) == rec["score"]
 
 
+def chunk_path_noise_grid(seed):
+    """The oracle's chunk-path noise1..5 sums (generateTerrainNoise as the exact
+    terrain runs it, 5x5 lattice per chunk) for the 15x15 chunks of a radius-7
+    region around (0,0), laid out on the 61x61 coarse grid at -28..32. Columns on
+    chunk borders are computed by up to four chunks; all of them must agree."""
+    L = po.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.or_chunk_noise_test.argtypes = [ctypes.c_int64, ctypes.c_int, ctypes.c_int] + [dp] * 5
+    grid = [np.full(61 * 61 * 17, np.nan), np.full(61 * 61 * 17, np.nan), np.full(61 * 61 * 17, np.nan),
+            np.full(61 * 61, np.nan), np.full(61 * 61, np.nan)]
+    for cx in range(-7, 8):
+        for cz in range(-7, 8):
+            o = [np.zeros(25 * 17), np.zeros(25 * 17), np.zeros(25 * 17), np.zeros(25), np.zeros(25)]
+            L.or_chunk_noise_test(seed, cx, cz, *[a.ctypes.data_as(dp) for a in o])
+            for i in range(5):
+                for j in range(5):
+                    col = (4 * cx + i + 28) * 61 + (4 * cz + j + 28)
+                    c = i * 5 + j
+                    for k in range(5):
+                        per = 17 if k < 3 else 1
+                        new = o[k][c * per:(c + 1) * per]
+                        old = grid[k][col * per:(col + 1) * per]
+                        if not np.isnan(old).all():
+                            assert np.array_equal(old.view(np.uint64), new.view(np.uint64)), (seed, cx, cz, i, j, k)
+                        grid[k][col * per:(col + 1) * per] = new
+    assert not any(np.isnan(g).any() for g in grid)
+    return grid
+
+
+def test_chunk_path_noise_matches_reference_coarse_noise():
+    """The chunk path's lattice noise (the input of the trilinear fill, the exact
+    scan and previews) equals, bit for bit, the reference's own coarse-grid noise
+    sums (coarsecore::generateAndScoreHost: perlin3Full17 for noise1..3 and
+    p20::perlin2 for noise4/5) at the same coarse coordinates."""
+    for rec in GOLDEN["chunk_noise"]:
+        grid = chunk_path_noise_grid(rec["seed"])
+        assert [hashlib.sha256(g.tobytes()).hexdigest() for g in grid] == rec["sha256"], rec["seed"]
+        assert _bits(grid[1][:17]) == rec["n2_col0"] and _bits(grid[4][:1]) == rec["n5_col0"]
+
+
 def test_splitmix_matches_reference():
     for rec in GOLDEN["splitmix"]:
         assert po.splitmix_seed(rec["sequence"], rec["attempt"]) == int(rec["seed"])
 
 
-@pytest.mark.skipif(po.ref() is None and not os.path.isdir("/root/reference"), reason="reference checkout absent")
+@pytest.mark.skipif(po.ref() is None and po.build_ref() is None, reason="reference checkout absent")
 def test_oracle_against_live_reference_random():
     """Extra random cases straight against the reference harness when it is built here."""
     R = po.ref() or (po.build_ref() and po.ref())
