@@ -37,6 +37,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 GOLDEN = 0x9E3779B97F4A7C15
+PROFILE_IDS = {"general": 0, "mega": 1, "record60": 2, "record80": 3}
+
+# DRAM bytes per world of one k_stage0_fast launch (dram__bytes_read.sum +
+# dram__bytes_write.sum from an ncu capture of an 8,192-world MEGA batch, 512x1
+# launch shape, divided by the worlds): the per-world generator cache (21,888 B) read
+# once, plus region records. It scales in proportion to the worlds.
+STAGE0_TRAFFIC_BYTES_PER_WORLD = 25708
 
 
 def parse():
@@ -50,8 +57,14 @@ def parse():
     p.add_argument("--radius", type=int, default=7)
     p.add_argument("--seed", type=int, default=20261203)
     p.add_argument("--plain-steps", type=int, default=2)
-    p.add_argument("--cpu-sample", type=int, default=1024, help="worlds for the CPU baseline sample")
-    p.add_argument("--ref-sample", type=int, default=256, help="worlds per reference-arm step")
+    p.add_argument("--ref-sample", type=int, default=256,
+                   help="worlds per CPU step: the first worlds of the matching GPU batch (reference arm and "
+                        "cpu_baseline)")
+    p.add_argument("--cpu-steps", type=int, default=4, help="CPU steps of the cpu_baseline sample")
+    p.add_argument("--ref-gpu-steps", type=int, default=2,
+                   help="batches through the reference worker's own GPU kernels (0: skip)")
+    p.add_argument("--sweep-seeds", type=int, default=1 << 26, help="seeds of the Stage0 scout sweep (0: skip)")
+    p.add_argument("--sweep-capacity", type=int, default=65536, help="worlds per Stage0 sweep batch")
     p.add_argument("--previews", type=int, default=30)
     p.add_argument("--served-ranges", type=int, default=4, help="range requests of --batch worlds in the served mix")
     p.add_argument("--served-chunk", type=int, default=16384, help="worlds per served range chunk (lane capacity)")
@@ -211,48 +224,128 @@ def stage0_fp64_ops(c):
         0.5 * column_fp64_ops(6) + 0.5 * column_fp64_ops(5))
 
 
-def cpu_baseline(args, seeds_start, n_worlds):
-    from oracle import pyoracle as po
+def cpu_sample_run(args, steps, warmup):
+    """The oracle's CPU pipeline on all host cores over a bounded sample of the GPU
+    arm's own seed stream: step k takes the first --ref-sample worlds of the GPU
+    arm's timed batch k (warm-up step w: of its warm-up batch w)."""
     import numpy as np
+    from oracle import pyoracle as po
     po.build()
     threads = os.cpu_count() or 1
-    seeds = np.arange(seeds_start, seeds_start + n_worlds, dtype=np.int64)
+    start = seed_start(args.seed, 0, 0)
+
+    def block(b):
+        base = start + b * args.batch
+        return np.arange(base, base + args.ref_sample, dtype=np.int64)
+
+    for w in range(warmup):
+        po.mega_pipeline(block(w), profile=PROFILE_IDS[args.profile], radius=args.radius, threads=threads)
     t0 = time.perf_counter()
-    counts, islands, _ = po.mega_pipeline(seeds, profile=1, radius=args.radius, threads=threads)
+    for k in range(steps):
+        po.mega_pipeline(block(args.warmup + k), profile=PROFILE_IDS[args.profile], radius=args.radius,
+                         threads=threads)
     dt = time.perf_counter() - t0
-    return n_worlds / dt, threads, dt, counts
+    sample = ("first %d of the %d worlds (x 8 centres) of each of %d GPU-arm timed batches, full MEGA pipeline"
+              % (args.ref_sample, args.batch, steps))
+    return args.ref_sample * steps / dt, threads, dt, sample
 
 
 def run_reference(args, dist):
-    """CPU reference arm: the oracle restatement of the reference pipeline on all host cores."""
+    """CPU reference arm: the oracle restatement of the reference pipeline on all
+    host cores, on the GPU arm's seed stream (a bounded sample of each batch)."""
     if dist.rank != 0:
         return
-    import numpy as np
-    from oracle import pyoracle as po
-    po.build()
-    threads = os.cpu_count() or 1
-    start = seed_start(args.seed, 0, 1)
-    for w in range(args.warmup):
-        s = np.arange(start + w * args.ref_sample, start + (w + 1) * args.ref_sample, dtype=np.int64)
-        po.mega_pipeline(s, profile=1, radius=args.radius, threads=threads)
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        base = start + (args.warmup + k) * args.ref_sample
-        s = np.arange(base, base + args.ref_sample, dtype=np.int64)
-        po.mega_pipeline(s, profile=1, radius=args.radius, threads=threads)
-    dt = time.perf_counter() - t0
-    v = args.ref_sample * args.steps / dt
+    v, threads, dt, sample = cpu_sample_run(args, args.steps, min(args.warmup, 1))
     line = {
         "impl": "reference", "metric": "seeds_per_s_mega_pipeline", "value": v, "unit": "worlds/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "mega_pipeline_consecutive_48bit_seeds", "profile": args.profile,
-                   "centers": 8, "exact_radius": args.radius, "worlds_per_step": args.ref_sample},
-        "cpu_baseline": {"value": v, "unit": "worlds/s", "cores": threads, "kind": "port",
-                         "sample": "%d consecutive worlds x 8 centres per step" % args.ref_sample},
+                   "centers": 8, "exact_radius": args.radius, "worlds_per_step": args.batch,
+                   "sampled_worlds_per_step": args.ref_sample},
+        "cpu_baseline": {"value": v, "unit": "worlds/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "worlds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def reference_gpu_leg(args, bsf, worker, blocks):
+    """The reference worker's own GPU kernels (compiled unmodified from its source,
+    driven in its stage0stream order, host P19 step included) against this
+    library's stage0stream response (bsf_stage0_filter) on the same seeds: worlds/s
+    of each, wall clock with host seeds in and records out, and the number of
+    region records that differ."""
+    import numpy as np
+    from oracle import pyoracle as po
+    if not os.path.exists(po.REF_CUBIN):
+        return {"unavailable": "reference GPU image oracle/_ref/ref_worker.cubin was not built"}
+    prof = PROFILE_IDS[args.profile]
+    n = len(blocks) - 1
+    with po.RefGpu(capacity=len(blocks[0])) as g:
+        g.stage0_batch(blocks[0], centers=8, profile=prof, research=False)  # warm-up (module load)
+        stage = np.zeros(3)
+        ref_out = []
+        t0 = time.perf_counter()
+        for b in blocks[1:]:
+            ref_out.append(g.stage0_batch(b, centers=8, profile=prof, research=False))
+            stage += g.last_ms()
+        ref_s = time.perf_counter() - t0
+    worker.stage0_filter(blocks[0])
+    t0 = time.perf_counter()
+    mine = [worker.stage0_filter(b) for b in blocks[1:]]
+    ours_s = time.perf_counter() - t0
+    bad = sum(int((a.reshape(-1, 16) != b.reshape(-1, 16)).any(axis=1).sum()) for a, b in zip(mine, ref_out))
+    worlds = sum(len(b) for b in blocks[1:])
+    return {
+        "what": "stage0stream response (P20 -> Upper -> Lower -> P19 -> coarse, 16-byte records) per batch of "
+                "%d worlds x 8 centres, host seeds in and records out" % len(blocks[0]),
+        "reference_worlds_per_s": worlds / ref_s, "ours_worlds_per_s": worlds / ours_s,
+        "ours_over_reference": ref_s / ours_s,
+        "reference_stage_ms_per_batch": {"stage0_kernels_and_copies": stage[0] / n, "host_p19": stage[1] / n,
+                                         "coarse_microbatches": stage[2] / n},
+        "batches": n, "mismatched_region_records": bad, "regions_compared": worlds * 8,
+        "reference_build": "native/src/gpu_p20_benchmark.cpp unmodified, nvcc -O3 --fmad=false --ftz=false "
+                           "--prec-div=true --prec-sqrt=true, sm_103a",
+    }
+
+
+def stage0_sweep_leg(args, bsf):
+    """Stage0 scout sweep: --sweep-seeds consecutive 48-bit seeds from a seeded start
+    through P20 -> Upper -> Lower at the origin region (one centre), survivors as a
+    seed list; with the oracle's verdict on sampled windows of the sweep."""
+    import numpy as np
+    from oracle import pyoracle as po
+    count = args.sweep_seeds
+    start = seed_start(args.seed, 0, 6)
+    prof = PROFILE_IDS[args.profile]
+    with bsf.Worker(capacity=args.sweep_capacity, profile=prof, centers=1, max_exact_radius=1) as w:
+        w.stage0_sweep(start + count, 3 * args.sweep_capacity)  # warm-up: graphs and caches
+        l0 = w.kernel_launches
+        t0 = time.perf_counter()
+        surv, total, c = w.stage0_sweep(start, count, cap=count // 2)
+        dt = time.perf_counter() - t0
+        launches = w.kernel_launches - l0
+    rng = np.random.default_rng(args.seed + 6)
+    gates = {0: (1, 5, 5), 1: (1, 8, 6), 2: (3, 19, 12), 3: (3, 19, 20)}[prof]
+    mismatches, audited = 0, 0
+    for off in rng.integers(0, count - 512, size=4):
+        seeds = np.arange(start + int(off), start + int(off) + 512, dtype=np.int64)
+        r = po.stage0_batch(seeds, centers=1, profile=prof).reshape(-1, 16)
+        want = seeds[(r[:, 0] >= gates[0]) & (r[:, 1] >= gates[1]) & (r[:, 2] >= gates[2])]
+        lo, hi = np.searchsorted(surv, seeds[0]), np.searchsorted(surv, seeds[-1], side="right")
+        got = surv[lo:hi]
+        mismatches += len(np.setxor1d(got, want))
+        audited += len(seeds)
+    return {
+        "workload": "%d consecutive 48-bit seeds from a seeded start, Stage0 gate at the origin region "
+                    "(profile %s)" % (count, args.profile),
+        "seeds_per_s": count / dt, "seconds": dt, "survivors": total,
+        "pass_rate": {"p20": c["p20_passed"] / count, "upper": c["upper_passed"] / count,
+                      "high": c["high_passed"] / count, "survivor_worlds": total / count},
+        "gpu_launches": launches, "batch_worlds": args.sweep_capacity,
+        "oracle_audit": {"seeds": audited, "mismatched_survivors": mismatches},
+        "screen_fallback_rate": c["fallback_tasks"] / max(1, c["screened_tasks"]),
+    }
 
 
 def served_form(args, bsf, start):
@@ -428,6 +521,7 @@ def main():
     totals = None
     stage = [0.0, 0.0, 0.0, 0.0]
     records = 0
+    dev_recs = []
     for s in range(K):
         counts, recs = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
         d = counts.as_dict()
@@ -435,6 +529,7 @@ def main():
         st = worker.last_stage_ms()
         stage = [a + b for a, b in zip(stage, st)]
         records += len(recs)
+        dev_recs.append(recs)
     e1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()
@@ -444,19 +539,25 @@ def main():
     ms_max = dist.max(ms)
     value = B * K * dist.world / (ms_max / 1e3)
 
-    # e2e: host seeds through the public API (H2D seeds, D2H counts + records inside).
-    host_start = seed_start(args.seed, dist.rank, 2)
-    host_blocks = [np.arange(host_start + s * B, host_start + (s + 1) * B, dtype=np.int64) for s in range(K + 1)]
-    worker.mega_search(host_blocks[K], radius=args.radius)
+    # e2e: the same seeds as the device-timed steps, from host memory through the
+    # public API (H2D seeds, D2H counts + records inside the timed region).
+    host_blocks = [d_seeds[W + s].cpu().numpy() for s in range(K)]
+    worker.mega_search(d_seeds[0].cpu().numpy(), radius=args.radius)
     dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_records = 0
+    e2e_recs = []
     for s in range(K):
         _, recs = worker.mega_search(host_blocks[s], radius=args.radius)
         e2e_records += len(recs)
+        e2e_recs.append(recs)
     torch.cuda.synchronize()
     e2e_s = dist.max(time.perf_counter() - t0)
+
+    def rec_keys(rs):
+        return [(r.seed, r.world_index, r.center_index, r.coarse, r.island.key()) for r in rs]
+    e2e_same = all(rec_keys(a) == rec_keys(b) for a, b in zip(dev_recs, e2e_recs))
     e2e_value = B * K * dist.world / e2e_s
     rec_bytes = __import__("ctypes").sizeof(bsf.MegaRecord)
     d2h = 8 * 8 + 4 * 4 + (e2e_records / max(1, K)) * (rec_bytes + 48)
@@ -504,6 +605,11 @@ def main():
             if args.mix_seconds > 0:
                 extras["served_mix"] = served_mix(args, bsf, seed_start(args.seed, dist.rank, 5),
                                                   served["worlds_per_s"])
+        if args.ref_gpu_steps > 0:
+            blocks = [d_seeds[min(W + s, steps_total - 1)].cpu().numpy() for s in range(args.ref_gpu_steps + 1)]
+            extras["reference_gpu"] = reference_gpu_leg(args, bsf, worker, blocks)
+        if args.sweep_seeds > 0:
+            extras["stage0_sweep"] = stage0_sweep_leg(args, bsf)
         # single-seed island previews (served request class): latency per preview
         lat = []
         for i in range(args.previews):
@@ -519,22 +625,12 @@ def main():
         ops = stage0_fp64_ops(totals) / K
         fp64_peak, fp32_peak = measured_peaks()
         achieved = ops / (stage0_ms / 1e3)
-        # DRAM bytes per launch of k_stage0_fast from an ncu capture of a smaller batch
-        # (dram__bytes_read.sum + dram__bytes_write.sum per world), scaled to this batch:
-        # the traffic is the per-world generator cache and region records, so it grows
-        # in proportion to the worlds.
-        traffic = None
-        tpath = os.path.join(ROOT, "profiles", "k_stage0_fast_mega_8192worlds.md")
-        if os.path.exists(tpath):
-            import re
-            m = re.search(r"traffic_bytes_per_world:\s*(\d+)", open(tpath).read())
-            if m:
-                traffic = int(m.group(1)) * B
+        traffic = STAGE0_TRAFFIC_BYTES_PER_WORLD * B
         cpu = None
         if not args.skip_extras:
-            v, cores, dt, _ = cpu_baseline(args, seed_start(args.seed, 0, 3), args.cpu_sample)
+            v, cores, dt, sample = cpu_sample_run(args, args.cpu_steps, 0)
             cpu = {"value": v, "unit": "worlds/s", "cores": cores, "kind": "port",
-                   "sample": "%d consecutive worlds x 8 centres, full MEGA pipeline, %.1f s" % (args.cpu_sample, dt)}
+                   "sample": sample + ", %.1f s" % dt}
         line = {
             "metric": "seeds_per_s_mega_pipeline", "value": value, "unit": "worlds/s", "n_gpus": dist.world,
             "steps": K, "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
@@ -544,12 +640,14 @@ def main():
                        "l2": "per-step working set (generator cache %.0f MB) exceeds L2" % (B * 21888 / 1e6),
                        "autotune": tune_report},
             "e2e": {"value": e2e_value, "unit": "worlds/s", "h2d_bytes_per_step": B * 8,
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "seeds": "the device-timed steps' seeds, from host memory",
+                    "records_equal_to_value_run": e2e_same},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "kernel": "k_stage0_fast", "achieved": achieved / 1e12,
                          "peak": fp32_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                          "traffic": traffic,
-                         "peak_source": "measured live: FP32 add issue rate of this GPU (library probe)",
+                         "peak_source": ("measured live by the library's own probe (independent FP32 add chains on "
+                                         "every SM); the provided measured peaks cover only HBM copy and bf16 GEMM"),
                          "work_model": ("reference-formulation FP64 ops per lattice column: 3D octave 22 + 21/cell + "
                                         "11/level, 2D octave 37, simplex octave 60, climate and shape 45, "
                                         "12 per density level"),
@@ -564,6 +662,9 @@ def main():
         if cpu:
             line["cpu_baseline"] = cpu
         line.update(extras)
+        rg = extras.get("reference_gpu", {})
+        if "ours_over_reference" in rg:
+            line["vs_reference_gpu"] = rg["ours_over_reference"]
         print(json.dumps(line))
     worker.close()
     dist.close()

@@ -103,11 +103,20 @@ class ServerStats(ctypes.Structure):
         return d
 
 
+class SweepCounts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "worlds", "regions", "p20_passed", "upper_passed", "high_passed", "survivors", "rng_fallbacks",
+        "screened_tasks", "fallback_tasks")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 REQ_RANGE, REQ_PREVIEW = 0, 1
 PENDING = 1
 
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
-           "bsf_set_mode", "bsf_stage0_filter", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
+           "bsf_set_mode", "bsf_stage0_filter", "bsf_stage0_sweep", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
            "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
@@ -138,6 +147,7 @@ def load(path=LIB_PATH):
     L.bsf_set_mode.argtypes = [vp, ctypes.c_int32]
     L.bsf_stage0_filter.argtypes = [vp, i64p, ctypes.c_uint32, u8p, ctypes.c_size_t]
     L.bsf_p20_filter.argtypes = [vp, i64p, ctypes.c_uint32, u8p, ctypes.c_size_t]
+    L.bsf_stage0_sweep.argtypes = [vp, ctypes.c_int64, ctypes.c_uint64, i64p, ctypes.c_uint64, u64p, P(SweepCounts)]
     L.bsf_chunk_bitmaps.argtypes = [vp, i64p, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, u8p, u64p]
     L.bsf_exact_scan.argtypes = [vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                  P(MatchSettings), P(Island)]
@@ -318,6 +328,20 @@ class Worker:
         self._check(load().bsf_stage0_filter(self._h, _p(seeds, ctypes.c_int64), len(seeds),
                                              _p(out, ctypes.c_uint8), out.nbytes))
         return out
+
+    def stage0_sweep(self, start_seed, count, cap=None):
+        """Stage0 scout sweep over `count` consecutive seeds from start_seed: the
+        surviving worlds' seeds (numpy int64, sweep order, at most cap), the total
+        survivor count and the stage pass counters."""
+        cap = int(count) if cap is None else int(cap)
+        out = np.zeros(max(cap, 1), np.int64)
+        n = ctypes.c_uint64(0)
+        c = SweepCounts()
+        start = int(start_seed)
+        start = start - (1 << 64) if start >= (1 << 63) else start
+        self._check(load().bsf_stage0_sweep(self._h, start, int(count), _p(out, ctypes.c_int64), cap,
+                                            ctypes.byref(n), ctypes.byref(c)))
+        return out[:min(cap, n.value)].copy(), n.value, c.as_dict()
 
     def p20_filter(self, seeds):
         seeds = np.ascontiguousarray(seeds, dtype=np.int64)

@@ -182,6 +182,11 @@ struct BsfHandle {
     int* dPrevMin = nullptr;
     int* dPrevMax = nullptr;
     int prevCap = 0;
+    SweepState sweep;                     // bsf_stage0_sweep (bsf_sweep.cu)
+    void* dSweepBase = nullptr;
+    std::int64_t* hSweepOut = nullptr;    // pinned copy of the survivor list
+    unsigned long long* hSweep = nullptr; // pinned: [0] start seed, [1] list total, [2..5] stage counters,
+                                          // [6..7] screen stats, [8] setup fallbacks
     std::int64_t* hSeeds = nullptr;  // pinned staging
     std::uint8_t* hOut = nullptr;
     std::size_t outBytes = 0;
@@ -493,11 +498,23 @@ void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seed
 // Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters.
 constexpr int kBatchGraphKernels = 6;
 
-cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
-    const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
-    const int variants =
-        (((get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0)) * 2 +
-         h->fs.forceExact) * 4 + h->cfg.profile;  // the profile's gates are kernel parameters of the graph
+// Batches of a Stage0 sweep between two host reads of the survivor list (the
+// list holds this many batches' worth, so it never overflows in between).
+constexpr int kSweepFlush = 8;
+// Kernels in one sweep-batch graph: seeds, setup, Stage0, P19, count, write, advance.
+constexpr int kSweepGraphKernels = 7;
+
+// Launch-shape, grid-shape, verification and profile state a graph was captured
+// with (the profile's gates are kernel parameters of the graph).
+int graph_variants(const BsfHandle* h) {
+    return (((get_stage0_fast_variant() * 64 + get_coarse_fast_variant()) * 2 + (h->persistent ? 1 : 0)) * 2 +
+            h->fs.forceExact) * 4 + h->cfg.profile;
+}
+
+// The cached graph of `key` on the handle's stream, captured from `enqueue` on a miss.
+template <typename F>
+cudaGraphExec_t cached_graph(BsfHandle* h, long long key, F&& enqueue) {
+    const int variants = graph_variants(h);
     for (const auto& g : h->graphs)
         if (g.first == key && g.second.stream == h->stream && g.second.variants == variants) return g.second.exec;
     const unsigned long long launchesBefore = h->launches.load();
@@ -505,7 +522,7 @@ cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
     std::shared_lock<std::shared_mutex> captureLock(capture_guard());
     check(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
     try {
-        enqueue_batch(h, n, hostSeeds ? 2 : 0, nullptr);
+        enqueue();
     } catch (...) {
         cudaStreamEndCapture(h->stream, &graph);
         if (graph) cudaGraphDestroy(graph);
@@ -523,6 +540,80 @@ cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
     }
     h->graphs.push_back({key, BsfHandle::CachedGraph{exec, h->stream, variants}});
     return exec;
+}
+
+cudaGraphExec_t batch_graph(BsfHandle* h, int n, bool hostSeeds) {
+    const long long key = static_cast<long long>(n) * 2 + (hostSeeds ? 1 : 0);
+    return cached_graph(h, key, [&]() { enqueue_batch(h, n, hostSeeds ? 2 : 0, nullptr); });
+}
+
+// One Stage0 sweep batch of n worlds: seeds from the device cursor, generator
+// setup, screened Stage0 (+ P19 fields), and the ordered survivor append.
+cudaGraphExec_t sweep_graph(BsfHandle* h, int n) {
+    const long long key = -1 - static_cast<long long>(n);  // batch graphs use keys >= 0
+    return cached_graph(h, key, [&]() {
+        launch_sweep_seeds(h->dSeeds, n, h->sweep, h->stream);
+        launch_world_init(h->dSeeds, n, h->cache, h->dCounters + 1, h->stream);
+        launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, nullptr, h->dCounters, 0, h->fs, h->stream,
+                           h->persistent);
+        launch_sweep_compact(h->dRegions, h->dSeeds, n, h->centers, h->prof, h->sweep, h->stream);
+    });
+}
+
+// Stage0 scout sweep over `count` consecutive seeds from `start`, in batches of
+// the handle's capacity. The survivor list is read back every kSweepFlush
+// batches; the list is in seed order, so the host only appends.
+void stage0_sweep(BsfHandle* h, std::int64_t start, std::uint64_t count, std::int64_t* out, std::uint64_t cap,
+                  std::uint64_t* nOut, bsf_sweep_counts* counts) {
+    if (!nOut || count == 0 || (!out && cap)) throw std::invalid_argument("bsf_stage0_sweep: bad count/output");
+    if (h->mode != BSF_MODE_QUEUED) throw std::invalid_argument("bsf_stage0_sweep runs in the queued form only");
+    unsigned long long* hs = h->hSweep;
+    hs[0] = static_cast<unsigned long long>(start);
+    check(cudaMemcpyAsync(h->sweep.next, hs, 8, cudaMemcpyHostToDevice, h->stream), "sweep start");
+    check(cudaMemsetAsync(h->sweep.total, 0, 8 * 5, h->stream), "memset");  // total + 4 stage counters
+    check(cudaMemsetAsync(h->dCounters, 0, 4 * sizeof(int), h->stream), "memset");
+    check(cudaMemsetAsync(h->fs.stats, 0, 4 * sizeof(unsigned long long), h->stream), "memset");
+    std::uint64_t remaining = count, written = 0, survivors = 0;
+    while (remaining) {
+        for (int b = 0; b < kSweepFlush && remaining; ++b) {
+            const int n = static_cast<int>(std::min<std::uint64_t>(remaining, static_cast<std::uint64_t>(h->capacity)));
+            check(cudaGraphLaunch(sweep_graph(h, n), h->stream), "sweep graph");
+            h->launches += kSweepGraphKernels;
+            remaining -= static_cast<std::uint64_t>(n);
+        }
+        check(cudaMemcpyAsync(hs + 1, h->sweep.total, 8, cudaMemcpyDeviceToHost, h->stream), "sweep total");
+        check(cudaStreamSynchronize(h->stream), "sweep");
+        const std::uint64_t total = hs[1];
+        if (total > h->sweep.outCap) throw std::runtime_error("sweep survivor list overflowed");
+        const std::uint64_t take = written < cap ? std::min<std::uint64_t>(total, cap - written) : 0;
+        if (take) {
+            check(cudaMemcpyAsync(h->hSweepOut, h->sweep.out, take * 8, cudaMemcpyDeviceToHost, h->stream),
+                  "survivors");
+            check(cudaStreamSynchronize(h->stream), "survivors");
+            std::memcpy(out + written, h->hSweepOut, take * 8);
+            written += take;
+        }
+        survivors += total;
+        check(cudaMemsetAsync(h->sweep.total, 0, 8, h->stream), "memset");
+    }
+    check(cudaMemcpyAsync(hs + 2, h->sweep.stage, 4 * 8, cudaMemcpyDeviceToHost, h->stream), "sweep counters");
+    check(cudaMemcpyAsync(hs + 6, h->fs.stats, 2 * 8, cudaMemcpyDeviceToHost, h->stream), "screen stats");
+    check(cudaMemcpyAsync(hs + 8, h->dCounters + 1, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "fallbacks");
+    check(cudaStreamSynchronize(h->stream), "sweep counters");
+    const int fallbacks = *reinterpret_cast<const int*>(hs + 8);
+    if (hs[5] != survivors) throw std::runtime_error("sweep survivor count mismatch");
+    *nOut = survivors;
+    if (counts) {
+        counts->worlds = count;
+        counts->regions = count * static_cast<std::uint64_t>(h->centers);
+        counts->p20_passed = hs[2];
+        counts->upper_passed = hs[3];
+        counts->high_passed = hs[4];
+        counts->survivors = survivors;
+        counts->rng_fallbacks = static_cast<std::uint64_t>(fallbacks);
+        counts->screened_tasks = hs[6];
+        counts->fallback_tasks = hs[7];
+    }
 }
 
 int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, uint32_t count,
@@ -715,6 +806,20 @@ void open_buffers(BsfHandle* h, const bsf_config& cfg) {
     h->prevCap = 16 * (2 * cfg.max_exact_radius + 1) * 16 * (2 * cfg.max_exact_radius + 1);
     h->alloc(reinterpret_cast<void**>(&h->dPrevMin), static_cast<std::size_t>(h->prevCap) * 4, "preview");
     h->alloc(reinterpret_cast<void**>(&h->dPrevMax), static_cast<std::size_t>(h->prevCap) * 4, "preview");
+    // Stage0 sweep: cursor, total and stage counters (64 B), per-block counts, and a
+    // survivor list that holds kSweepFlush batches (a batch has at most n survivors)
+    const std::size_t blocks = static_cast<std::size_t>(sweep_blocks(h->capacity));
+    h->sweep.outCap = static_cast<unsigned long long>(kSweepFlush) * n;
+    const std::size_t sweepBytes = 64 + ((blocks * 4 + 255) / 256) * 256 + h->sweep.outCap * 8;
+    h->alloc(&h->dSweepBase, sweepBytes, "sweep");
+    if (!h->dry) {
+        unsigned char* b = static_cast<unsigned char*>(h->dSweepBase);
+        h->sweep.next = reinterpret_cast<unsigned long long*>(b);
+        h->sweep.total = h->sweep.next + 1;
+        h->sweep.stage = h->sweep.next + 2;  // 4 counters
+        h->sweep.blockCounts = reinterpret_cast<int*>(b + 64);
+        h->sweep.out = reinterpret_cast<std::int64_t*>(b + 64 + ((blocks * 4 + 255) / 256) * 256);
+    }
 }
 
 // Constant tables and kernel attributes, once per device: handles opened later
@@ -782,6 +887,8 @@ void* bsf_open(const bsf_config* cfgIn) {
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hPinned), 16 * sizeof(unsigned long long)), "pinned counters");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
               "pinned output");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hSweep), 16 * sizeof(unsigned long long)), "pinned sweep");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hSweepOut), h->sweep.outCap * 8), "pinned sweep list");
         check(cudaStreamSynchronize(h->stream), "open");
         h->ok = true;
     } catch (const std::exception& e) {
@@ -800,7 +907,7 @@ void bsf_close(void* hv) {
     void* dev[] = {h->dSeeds, h->cache.perms, h->cache.offsets, h->dRegions, h->dCoarseQueue, h->dCounters,
                    h->dSigns, h->dLabels, h->dStats, h->dOut, h->dHashes, h->dStageCounts, h->dExactQueue,
                    h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax, h->fs.p19Queue, h->fs.highest,
-                   h->fs.p19Count, h->fs.stats};
+                   h->fs.p19Count, h->fs.stats, h->dSweepBase};
     for (void* p : dev)
         if (p) cudaFree(p);
     for (auto& e : h->ev)
@@ -813,6 +920,8 @@ void bsf_close(void* hv) {
     if (h->hSeeds) cudaFreeHost(h->hSeeds);
     if (h->hOut) cudaFreeHost(h->hOut);
     if (h->hPinned) cudaFreeHost(h->hPinned);
+    if (h->hSweep) cudaFreeHost(h->hSweep);
+    if (h->hSweepOut) cudaFreeHost(h->hSweepOut);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1029,6 +1138,14 @@ int bsf_mega_search_device(void* hv, const int64_t* dSeeds, uint32_t count, int3
     return guarded(hv, [&](BsfHandle* h) {
         return mega_batch(h, dSeeds, false, static_cast<cudaStream_t>(stream), count, radius, s, records, recordsCap,
                           recordsCount, counts);
+    });
+}
+
+int bsf_stage0_sweep(void* hv, int64_t startSeed, uint64_t count, int64_t* survivors, uint64_t cap,
+                     uint64_t* nSurvivors, bsf_sweep_counts* counts) {
+    return guarded(hv, [&](BsfHandle* h) {
+        stage0_sweep(h, startSeed, count, survivors, cap, nSurvivors, counts);
+        return BSF_OK;
     });
 }
 

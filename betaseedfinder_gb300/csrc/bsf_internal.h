@@ -135,6 +135,22 @@ void init_coarse_fast();
 void launch_coarse_signs_fast(const StateCache& cache, const RegionRef* dQueue, const int* dCount, int maxCount,
                               std::uint32_t* dSigns, unsigned long long* stats, cudaStream_t stream,
                               bool persistent = true, bool forceExact = false);
+// Stage0 sweep state on the device (bsf_sweep.cu): a seed cursor, the running
+// survivor total and list, per-block survivor counts of the current batch and
+// the stage pass counters.
+struct SweepState {
+    unsigned long long* next = nullptr;    // first seed of the next batch
+    unsigned long long* total = nullptr;   // survivors in `out` so far
+    int* blockCounts = nullptr;            // [sweep_blocks(capacity)]
+    unsigned long long* stage = nullptr;   // [0] P20, [1] +Upper, [2] +high (regions), [3] surviving worlds
+    std::int64_t* out = nullptr;           // survivor seeds in seed order
+    unsigned long long outCap = 0;
+};
+int sweep_blocks(int n);
+void launch_sweep_seeds(std::int64_t* dSeeds, int n, const SweepState& st, cudaStream_t stream);
+// Counts the batch's gate passes and appends its surviving worlds' seeds, in order.
+void launch_sweep_compact(const RegionInfo* dRegions, const std::int64_t* dSeeds, int n, int centers,
+                          const Profile& prof, const SweepState& st, cudaStream_t stream);
 // Persistent coarse-score grid for a queue of maxCount regions: label/stat scratch
 // is per CTA (COARSE_CELLS ints of labels, 2 * COARSE_CELLS of stats) and the
 // union-find retry-bound flag (one int) follows the stat scratch.

@@ -166,8 +166,10 @@ __global__ void __launch_bounds__(INIT_LANES) k_world_init(const std::int64_t* _
                     j = static_cast<int>((static_cast<std::uint64_t>(bound) * r) >> 31);
                 } else {
                     std::uint32_t v = r % static_cast<std::uint32_t>(bound);
-                    // Java nextInt redraws while bits - val + (bound-1) overflows;
-                    // each redraw has probability < 2^-23, capped defensively.
+                    // Java nextInt redraws while bits - val + (bound-1) overflows. A
+                    // draw is rejected with probability (2^31 mod bound) / 2^31 < 2^-23
+                    // (bound <= 256), so the 64-redraw cap is reached with probability
+                    // below 2^-1472 per draw: unreachable, and the rebuild stays exact.
                     for (int guard = 0; guard < 64 &&
                          static_cast<std::int32_t>(r - v + static_cast<std::uint32_t>(bound - 1)) < 0; ++guard) {
                         s = lcg_step(s);

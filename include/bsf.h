@@ -107,6 +107,25 @@ int bsf_stage0_filter(void* h, const int64_t* seeds, uint32_t count, uint8_t* ou
  * GpuP20Scout, src/GpuP20Scout.java:45-93). */
 int bsf_p20_filter(void* h, const int64_t* seeds, uint32_t count, uint8_t* out, size_t out_len);
 
+/* Stage0 scout sweep: `count` consecutive world seeds start_seed, start_seed+1, ...
+ * (64-bit wrap-around), each at the handle's centres, through P20 -> Upper ->
+ * Lower under the handle's profile. A world survives when one of its regions
+ * passes the P20, Upper and high gates: the regions the app sends on to P19,
+ * i.e. rejectStage 0 or >= 5 (src/IslandSearchEngine.java:1368-1376; the
+ * per-region values are the stage0stream records' p20/upper/high,
+ * gpu_p20_benchmark.cpp:7421-7454). The survivors' seeds are written in
+ * increasing sweep order, at most `cap` of them; *n_survivors receives the total
+ * (which may exceed cap). Runs in the queued form; count may exceed the handle's
+ * capacity (the sweep runs in batches of capacity worlds). */
+typedef struct bsf_sweep_counts {
+    uint64_t worlds, regions;
+    uint64_t p20_passed, upper_passed, high_passed; /* regions passing P20, P20+Upper, P20+Upper+high */
+    uint64_t survivors;                             /* worlds with a region through all three gates */
+    uint64_t rng_fallbacks, screened_tasks, fallback_tasks;
+} bsf_sweep_counts;
+int bsf_stage0_sweep(void* h, int64_t start_seed, uint64_t count, int64_t* survivors, uint64_t cap,
+                     uint64_t* n_survivors, bsf_sweep_counts* counts);
+
 /* BetaTerrain173.generateChunkBaseTerrain (src/beta173/BetaTerrain173.java:120-138)
  * reduced to a stone bitmap: bit (x*16+z)*128+y of 4096 bytes per seed, LSB
  * first, plus a 64-bit hash per bitmap (sum over the 512 little-endian words w_i
@@ -288,8 +307,11 @@ int bsf_server_get_stats(void* s, bsf_server_stats* out);
  * loads the library keeps until the process exits; count beyond the maximum
  * returns BSF_E_LIMIT. The first call on each device does a one-time set-up
  * (constant tables, the scratch address) and should come before any stream
- * capture. All calls share the one array: calls whose work overlaps on the
- * GPU race. err (optional, err_len bytes) receives a message on failure. */
+ * capture. That set-up is kept for the life of the process: the entry point
+ * assumes the device (its primary context) is not reset after the first call,
+ * since a reset would leave a stale scratch address and empty constant tables.
+ * All calls share the one array: calls whose work overlaps on the GPU race.
+ * err (optional, err_len bytes) receives a message on failure. */
 #define BSF_NOALLOC_MAX_WORLDS 256u
 int bsf_chunk_bitmaps_noalloc(const int64_t* d_seeds, uint32_t count, int32_t chunk_x, int32_t chunk_z,
                               uint8_t* d_bitmaps, uint64_t* d_hashes, void* stream, char* err, size_t err_len);

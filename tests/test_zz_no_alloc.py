@@ -28,10 +28,14 @@ def _bind():
 
 
 def test_noalloc_matches_allocating_entry_point_twice():
+    """Calls in a row, against bsf_chunk_bitmaps: a partial call, one at the size
+    limit, then a smaller call at another chunk, which must ignore what the larger
+    call left in the shared scratch array. A repeat of the last call takes no
+    device memory (the free memory the driver reports does not change)."""
     torch = pytest.importorskip("torch")
     noalloc = _bind()
     stream = torch.cuda.current_stream().cuda_stream
-    calls = [(200, 0, 0, 101), (256, -3, 5, 202)]  # the second call is at the size limit
+    calls = [(200, 0, 0, 101), (256, -3, 5, 202), (17, 9, -4, 303)]
     for n, cx, cz, salt in calls:
         start = int(np.random.default_rng(salt).integers(0, 2 ** 48 - n))
         seeds = np.arange(start, start + n, dtype=np.int64)
@@ -46,6 +50,13 @@ def test_noalloc_matches_allocating_entry_point_twice():
             bm, h = w.chunk_bitmaps(seeds, cx, cz)
         assert np.array_equal(d_bm.cpu().numpy(), bm)
         assert np.array_equal(d_h.cpu().numpy().view(np.uint64), h)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    rc = noalloc(d_seeds.data_ptr(), n, cx, cz, d_bm.data_ptr(), d_h.data_ptr(), stream, err, 256)
+    assert rc == 0, err.value
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(d_bm.cpu().numpy(), bm)
 
 
 def test_noalloc_rejects_counts_beyond_its_scratch():
