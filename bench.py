@@ -65,6 +65,10 @@ def parse():
                    help="batches through the reference worker's own GPU kernels (0: skip)")
     p.add_argument("--sweep-seeds", type=int, default=1 << 26, help="seeds of the Stage0 scout sweep (0: skip)")
     p.add_argument("--sweep-capacity", type=int, default=65536, help="worlds per Stage0 sweep batch")
+    p.add_argument("--coarse-cpu-regions", type=int, default=48, help="regions of the coarse CPU baselines")
+    p.add_argument("--jobs", type=int, default=64, help="skewed concurrent range jobs (0: skip)")
+    p.add_argument("--plain-jobs", type=int, default=6, help="of those, jobs rerun through the plain form")
+    p.add_argument("--r3-steps", type=int, default=3, help="timed batches at exact radius 3 (0: skip)")
     p.add_argument("--previews", type=int, default=30)
     p.add_argument("--served-ranges", type=int, default=4, help="range requests of --batch worlds in the served mix")
     p.add_argument("--served-chunk", type=int, default=16384, help="worlds per served range chunk (lane capacity)")
@@ -458,15 +462,29 @@ def served_mix(args, bsf, start, capacity_wps):
                 tickets.append((kind, 0, srv.submit_preview(a, 0, 0, b)))
             else:
                 tickets.append((kind, b, srv.submit_range(np.arange(a, a + b, dtype=np.int64), radius=args.radius)))
-        for kind, n, tk in tickets:
+        audit_ranges, audit_previews = [], []
+        for idx, ((kind, n, tk), req) in enumerate(zip(tickets, reqs)):
             r = srv.wait(tk, 300)
             if r.status != 0:
                 raise RuntimeError("served request failed: " + srv.last_error())
             lat[kind].append(r.latency_ms)
             worlds += n
+            # sampled audit, read back after the request finished: 1% of every range's
+            # worlds (world index divisible by 100), and one preview in 50
+            if kind == "preview":
+                if len(lat["preview"]) % 50 == 1:
+                    isl = r.island
+                    cells = (isl.max_x - isl.min_x + 1) * (isl.max_z - isl.min_z + 1) if isl.found else 0
+                    cols = srv.preview_columns(tk, cells) if cells else (None, None)
+                    audit_previews.append((req[2], req[3], isl.key(), cols))
+            else:
+                keep = [(x.world_index, x.center_index, x.island.key()) for x in srv.records(tk)
+                        if x.world_index % 100 == 0]
+                audit_ranges.append((req[2], n, keep))
             srv.release(tk)
         elapsed = time.perf_counter() - t0
         st = srv.stats()
+    audit = served_audit(args, audit_ranges, audit_previews)
 
     def pct(v, q):
         v = sorted(v)
@@ -478,7 +496,126 @@ def served_mix(args, bsf, start, capacity_wps):
         "latency_ms": {k: {"n": len(v), "p50": pct(v, 0.5), "p99": pct(v, 0.99), "p999": pct(v, 0.999)}
                        for k, v in lat.items()},
         "scaled": "ranges 2^12-2^16 and sweeps 2^17 worlds (the workload's 2^24-2^32 / 2^36 scaled to a bench run)",
+        "audit": audit,
     }
+
+
+def served_audit(args, ranges, previews):
+    """The oracle's answers for the sampled part of a served mix: for every range
+    or sweep, the exact-stage regions and islands of its worlds whose index is
+    divisible by 100; for every sampled preview, the island and its columns."""
+    import numpy as np
+    from oracle import pyoracle as po
+    threads = os.cpu_count() or 1
+    prof = PROFILE_IDS[args.profile]
+    mismatches, worlds = 0, 0
+    for base, n, got in ranges:
+        idx = np.arange(0, n, 100, dtype=np.int64)
+        seeds = (base + idx).astype(np.int64)
+        _, isl, reg = po.mega_pipeline(seeds, profile=prof, radius=args.radius, threads=threads)
+        want = [(int(idx[r // 8]), int(r % 8), i.key()) for i, r in zip(isl, reg)]
+        mismatches += len(set(want) ^ set(got))
+        worlds += len(seeds)
+    pmis = 0
+    for seed, radius, key, (mn, mx) in previews:
+        o, omn, omx = po.preview(seed, 0, 0, radius)
+        same = o.key() == key and (not o.found or (np.array_equal(omn, mn) and np.array_equal(omx, mx)))
+        pmis += 0 if same else 1
+    return {"range_worlds_audited": worlds, "range_mismatched_regions": mismatches,
+            "previews_audited": len(previews), "preview_mismatches": pmis,
+            "sample": "1% of each range's worlds (index divisible by 100); one preview in 50"}
+
+
+def coarse_cpu_leg(args, records34, seeds):
+    """The coarse stage on the host cores, two ways, on the coarse-evaluated regions
+    of a GPU batch: the full 61x61x17 scorer and the Java app's component-lazy P17
+    scorer (both oracle restatements). Both must give the GPU's score."""
+    import concurrent.futures
+    import numpy as np
+    from oracle import pyoracle as po
+    r = records34.reshape(-1, 34)
+    coarse = r[:, 4].astype(np.int64) | (r[:, 5].astype(np.int64) << 8)
+    evaluated = np.flatnonzero((r[:, 3] != 0) & (r[:, 7] == 0))[:args.coarse_cpu_regions]
+    if len(evaluated) == 0:
+        return {"unavailable": "no coarse-evaluated region in the batch"}
+    jobs = [(int(seeds[i // 8]), i % 8) for i in evaluated]
+    cx = (0, 15, 0, 15, -15, -15, 0, 15)
+    cz = (0, 0, 15, 15, 0, 15, -15, -15)
+    threads = os.cpu_count() or 1
+    out = {}
+    for name, fn in (("full", lambda j: po.coarse_score(j[0], cx[j[1]], cz[j[1]])),
+                     ("lazy_p17", lambda j: po.coarse_score_lazy(j[0], cx[j[1]], cz[j[1]])[0])):
+        t0 = time.perf_counter()
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            scores = list(ex.map(fn, jobs))
+        dt = time.perf_counter() - t0
+        out[name] = {"regions_per_s": len(jobs) / dt,
+                     "mismatches_vs_gpu": int(sum(a != b for a, b in zip(scores, coarse[evaluated])))}
+    out.update({"regions": len(jobs), "cores": threads, "kind": "port",
+                "sample": "the first %d coarse-evaluated regions of the last timed GPU batch" % len(jobs),
+                "lazy_over_full": out["lazy_p17"]["regions_per_s"] / out["full"]["regions_per_s"]})
+    return out
+
+
+def skewed_jobs_leg(args, bsf):
+    """Skewed concurrent range jobs: --jobs jobs of log-uniform 2^11..2^15 worlds (the
+    workload's 2^20..2^30 scaled to a bench run), each with one of the four hunt
+    profiles, an exact radius of 3..9 and an island-volume threshold of its own,
+    all submitted at once to one served pool (continuous batching, graph-captured
+    batches, autotuned launch shapes); then the first --plain-jobs of them again
+    through the plain stage-by-stage form, one after another. Records must agree."""
+    import numpy as np
+    rng = np.random.default_rng(args.seed + 4)
+    base = seed_start(args.seed, 0, 7)
+    jobs = []
+    for j in range(args.jobs):
+        n = int(2 ** rng.uniform(11, 15))
+        jobs.append({"start": base, "n": n, "profile": int(rng.integers(0, 4)), "radius": int(rng.integers(3, 10)),
+                     "min_blocks": int(rng.choice([300, 1000, 3000, 10000]))})
+        base += n
+    total = sum(j["n"] for j in jobs)
+    served = []
+    with bsf.Server(profile=PROFILE_IDS[args.profile], chunk_worlds=min(args.batch, args.served_chunk),
+                    max_lanes=args.served_lanes) as srv:
+        warm = srv.submit_range(np.arange(base, base + 4096, dtype=np.int64), radius=7)
+        srv.wait(warm, 120)
+        srv.release(warm)
+        t0 = time.perf_counter()
+        tickets = [srv.submit_range(np.arange(j["start"], j["start"] + j["n"], dtype=np.int64), radius=j["radius"],
+                                    settings=bsf.default_match_settings(min_blocks=j["min_blocks"]),
+                                    profile=j["profile"]) for j in jobs]
+        for tk in tickets:
+            r = srv.wait(tk, 600)
+            if r.status != 0:
+                raise RuntimeError("skewed job failed: " + srv.last_error())
+            served.append([(x.world_index, x.center_index, x.island.key()) for x in srv.records(tk)])
+            srv.release(tk)
+        served_s = time.perf_counter() - t0
+    plain_jobs = jobs[:args.plain_jobs]
+    mism = 0
+    with bsf.Worker(capacity=args.served_chunk, profile=PROFILE_IDS[args.profile], centers=8,
+                    max_exact_radius=24) as w:
+        w.set_mode(bsf.MODE_PLAIN)
+        w.mega_search(np.arange(base, base + 1024, dtype=np.int64), radius=7)  # warm-up
+        t0 = time.perf_counter()
+        for k, j in enumerate(plain_jobs):
+            w.set_profile(j["profile"])
+            ms = bsf.default_match_settings(min_blocks=j["min_blocks"])
+            got = []
+            for off in range(0, j["n"], args.served_chunk):
+                m = min(args.served_chunk, j["n"] - off)
+                seeds = np.arange(j["start"] + off, j["start"] + off + m, dtype=np.int64)
+                _, recs = w.mega_search(seeds, radius=j["radius"], settings=ms)
+                got += [(x.world_index + off, x.center_index, x.island.key()) for x in recs]
+            mism += len(set(got) ^ set(served[k]))
+        plain_s = time.perf_counter() - t0
+    plain_worlds = sum(j["n"] for j in plain_jobs)
+    return {"jobs": len(jobs), "worlds": total, "served_worlds_per_s": total / served_s,
+            "plain_jobs": len(plain_jobs), "plain_worlds_per_s": plain_worlds / plain_s,
+            "served_over_plain": (total / served_s) / (plain_worlds / plain_s),
+            "mismatched_records_vs_plain": mism,
+            "lengths": "log-uniform 2^11..2^15 worlds (the workload's 2^20..2^30 scaled to a bench run)",
+            "profiles_used": sorted({j["profile"] for j in jobs}), "radii_used": sorted({j["radius"] for j in jobs})}
 
 
 def main():
@@ -605,6 +742,24 @@ def main():
             if args.mix_seconds > 0:
                 extras["served_mix"] = served_mix(args, bsf, seed_start(args.seed, dist.rank, 5),
                                                   served["worlds_per_s"])
+        if args.r3_steps > 0:
+            # the same pipeline with the exact stage at radius 3 (a 7x7-chunk window)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            isl3 = 0
+            for s in range(args.r3_steps):
+                c3, r3 = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=3, stream=sptr)
+                isl3 += c3.islands
+            torch.cuda.synchronize()
+            extras["radius3"] = {"worlds_per_s": B * args.r3_steps / (time.perf_counter() - t0),
+                                 "islands": isl3, "worlds": B * args.r3_steps,
+                                 "note": "wall clock through bsf_mega_search_device, exact radius 3"}
+        if args.coarse_cpu_regions > 0:
+            worker.mega_search_device(d_seeds[W].data_ptr(), B, radius=args.radius, stream=sptr)
+            extras["coarse_cpu_baselines"] = coarse_cpu_leg(args, worker.last_region_records(B),
+                                                            d_seeds[W].cpu().numpy())
+        if args.jobs > 0:
+            extras["skewed_jobs"] = skewed_jobs_leg(args, bsf)
         if args.ref_gpu_steps > 0:
             blocks = [d_seeds[min(W + s, steps_total - 1)].cpu().numpy() for s in range(args.ref_gpu_steps + 1)]
             extras["reference_gpu"] = reference_gpu_leg(args, bsf, worker, blocks)

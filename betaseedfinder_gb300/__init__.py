@@ -118,7 +118,7 @@ PENDING = 1
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_stage0_sweep", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
-           "bsf_kernel_launches", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
+           "bsf_kernel_launches", "bsf_device_summary", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
            "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_last_region_records", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",

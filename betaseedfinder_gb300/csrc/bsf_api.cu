@@ -1262,6 +1262,16 @@ int bsf_measure_peaks(double* ops) {
     }
 }
 
+int bsf_device_summary(int32_t device, char* out, size_t outLen) {
+    if (!out || outLen == 0) return BSF_E_ARG;
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSF_E_CUDA;
+    std::snprintf(out, outLen, "GPU: %s\nArchitecture: sm_%d%d\nCompute units: %d\nGlobal memory: %g GiB\n",
+                  prop.name, prop.major, prop.minor, prop.multiProcessorCount,
+                  static_cast<double>(prop.totalGlobalMem) / (1024.0 * 1024.0 * 1024.0));
+    return BSF_OK;
+}
+
 uint64_t bsf_kernel_launches(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     return h ? h->launches.load() : 0;

@@ -204,9 +204,10 @@ constexpr float OCTAVE3_ABS_MAX = 1.55f;
 // Simplex sample with exact FP64 lattice geometry and an FP32 kernel: the
 // offsets d11..d16 are FP64 (they cancel large coordinates), the falloff and
 // gradients are FP32 tracked with bounds. Returns 70*(n0+n1+n2) with its bound.
-__device__ __forceinline__ float simplex_corner(float x, float z, int g, float& err) {
-    // x, z carry error <= u|.| (rounded exact offsets)
-    Fe X{x, fabsf(x) * U}, Z{z, fabsf(z) * U};
+__device__ __forceinline__ float simplex_corner(float x, float z, int g, float& err, float eg = 0.0f) {
+    // x, z carry error <= u|.| + eg (rounded offsets, eg > 0 when they come from
+    // the double-float geometry below)
+    Fe X{x, fabsf(x) * U + eg}, Z{z, fabsf(z) * U + eg};
     Fe t = fe_sub(fe_sub(Fe{0.5f, 0.0f}, fe_mul(X, X)), fe_mul(Z, Z));
     if (fabsf(t.v) <= t.e) {
         // the FP64 branch t < 0 may differ; the contribution is at most (|t|+e)^4 * 2
@@ -269,6 +270,119 @@ static __device__ __noinline__ Fe simplex2f(const Gen& s, double xs, double zs) 
     return Fe{v, 70.0f * (err + 2.0f * fabsf(sum) * U) + fabsf(v) * U};
 }
 
+// ---- simplex lattice geometry in double-float --------------------------------
+// The geometry of a simplex sample (skew, cell floors, the corner order and the
+// corner offsets) decides which gradients are read, so the reference's FP64
+// values must pick the same cell. GB300's FP64 pipe is 1/64 of its FP32 rate and
+// the climate's ten octaves per column are the screened kernels' main FP64 load,
+// so the geometry runs here on pairs of floats (h + l, ~48 bits): exact products
+// by FMA, error-free sums (Knuth's two-sum, Dekker's fast two-sum), after
+// Dekker (1971) and the double-double algorithms of Hida, Li and Bailey (2001).
+// Every value it yields is within 2^-32 of the real value of the reference
+// expression for |values| < 2^10 (about ten pair operations of relative error
+// 2^-46 each, inputs split at 2^-48), and the reference's FP64 values are
+// within 2^-40 of it. A floor
+// or the corner-order comparison whose argument lies within SIMPLEX_EPS = 2^-28
+// of its decision point is left to the FP64 path; every other decision equals
+// the FP64 one. The offsets, rounded to FP32, then carry u|x| + 2^-28.
+constexpr float SIMPLEX_EPS = 3.7252903e-9f;  // 2^-28
+
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    DF s = two_sum(a.h, b.h);
+    const DF t = two_sum(a.l, b.l);
+    s.l = s.l + t.h;
+    s = fast_two_sum(s.h, s.l);
+    s.l = s.l + t.l;
+    return fast_two_sum(s.h, s.l);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_mul_f(float a, DF b) {  // a * (b.h + b.l)
+    const float p = a * b.h;
+    float e = __fmaf_rn(a, b.h, -p);
+    e = __fmaf_rn(a, b.l, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    const float p = a.h * b.h;
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_of(double x) {  // split of an FP64 value (2^-48 relative)
+    const float h = __double2float_rn(x);
+    return DF{h, __double2float_rn(x - static_cast<double>(h))};
+}
+// The reference's simplex floor (v > 0 ? (int)v : (int)v - 1) of a pair value;
+// false when the value is within SIMPLEX_EPS of an integer, where that floor and
+// the FP64 rounding could disagree. n = floor(v.h); v lies in [n - |v.l|, n + 1),
+// and its distances to n and n + 1 are taken with exact two-sums, so they are
+// accurate to far below SIMPLEX_EPS however close to an integer v is.
+__device__ __forceinline__ bool df_floor(DF v, int& out) {
+    const float n = floorf(v.h);
+    const DF a = two_sum(v.h, -n);
+    const DF b = two_sum(v.h, -(n + 1.0f));
+    const float to_n = a.h + (a.l + v.l);     // v - n
+    const float to_n1 = b.h + (b.l + v.l);    // v - (n + 1)
+    out = static_cast<int>(n) + (to_n < 0.0f ? -1 : 0) + (to_n1 >= 0.0f ? 1 : 0);
+    return fabsf(to_n) > SIMPLEX_EPS && fabsf(to_n1) > SIMPLEX_EPS;
+}
+
+// simplex2f with the geometry in double-float (xs = X * sx, zs = Z * sx for the
+// integer block coordinates X, Z); false when a decision is too close to call,
+// in which case the caller takes the FP64 geometry.
+static __device__ __noinline__ bool simplex2f_df(const Gen& s, int bx, int bz, double sx, Fe& out) {
+    constexpr double F = 0.3660254037844386;
+    constexpr double G = 0.21132486540518713;
+    constexpr float FH = static_cast<float>(F), FL = static_cast<float>(F - static_cast<double>(FH));
+    constexpr float GH = static_cast<float>(G), GL = static_cast<float>(G - static_cast<double>(GH));
+    constexpr double G1 = G - 1.0, G2 = 2.0 * G - 1.0;  // corner offsets' constants, split like G
+    constexpr float G1H = static_cast<float>(G1), G1L = static_cast<float>(G1 - static_cast<double>(G1H));
+    constexpr float G2H = static_cast<float>(G2), G2L = static_cast<float>(G2 - static_cast<double>(G2H));
+    const DF sxd = df_of(sx);
+    const DF d5 = df_add(df_mul_f(static_cast<float>(bx), sxd), df_of(s.a));
+    const DF d6 = df_add(df_mul_f(static_cast<float>(bz), sxd), df_of(s.b));
+    const DF d7 = df_mul(df_add(d5, d6), DF{FH, FL});
+    int j1, k1;
+    if (!df_floor(df_add(d5, d7), j1) || !df_floor(df_add(d6, d7), k1)) return false;
+    const DF d8 = df_mul_f(static_cast<float>(j1 + k1), DF{GH, GL});
+    const DF d11 = df_add(d5, df_add(DF{-static_cast<float>(j1), 0.0f}, d8));
+    const DF d12 = df_add(d6, df_add(DF{-static_cast<float>(k1), 0.0f}, d8));
+    const DF diff = df_add(d11, df_neg(d12));
+    if (fabsf(diff.h) <= SIMPLEX_EPS) return false;
+    const int b0 = diff.h > 0.0f ? 1 : 0;
+    const int b1 = 1 - b0;
+    const DF d13 = df_add(d11, b0 ? DF{G1H, G1L} : DF{GH, GL});
+    const DF d14 = df_add(d12, b1 ? DF{G1H, G1L} : DF{GH, GL});
+    const DF d15 = df_add(d11, DF{G2H, G2L});
+    const DF d16 = df_add(d12, DF{G2H, G2L});
+    const int l1 = j1 & 255;
+    const int i2 = k1 & 255;
+    const int g0 = P(s.p, l1 + P(s.p, i2)) % 12;
+    const int g1 = P(s.p, l1 + b0 + P(s.p, i2 + b1)) % 12;
+    const int g2 = P(s.p, l1 + 1 + P(s.p, i2 + 1)) % 12;
+    float err = 0.0f;
+    const float n0 = simplex_corner(d11.h + d11.l, d12.h + d12.l, g0, err, SIMPLEX_EPS);
+    const float n1 = simplex_corner(d13.h + d13.l, d14.h + d14.l, g1, err, SIMPLEX_EPS);
+    const float n2 = simplex_corner(d15.h + d15.l, d16.h + d16.l, g2, err, SIMPLEX_EPS);
+    const float sum = n0 + n1 + n2;
+    const float v = 70.0f * sum;
+    out = Fe{v, 70.0f * (err + 2.0f * fabsf(sum) * U) + fabsf(v) * U};
+    return true;
+}
+
 // Climate (temperature, rain) with bounds (WorldChunkManager173.java:95-126).
 __device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe& temperature, Fe& rain) {
     const double X = static_cast<double>(bx);
@@ -289,7 +403,9 @@ __device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe&
             if (o < count[grp]) {
                 const double sx = d2 * d7;
                 const float w = static_cast<float>(0.55 / d6);  // 0.55 * 2^k: FP32 rounding of w tracked below
-                const Fe s = simplex2f(t(ST_TEMP + base[grp] + o), X * sx, Z * sx);
+                const Gen g = t(ST_TEMP + base[grp] + o);
+                Fe s;
+                if (!simplex2f_df(g, bx, bz, sx, s)) s = simplex2f(g, X * sx, Z * sx);
                 const Fe term{s.v * w, s.e * w + fabsf(s.v * w) * 2.0f * U};
                 acc = fe_add(acc, term);
                 d7 *= octScale[grp];

@@ -68,9 +68,60 @@ int parse_profile(const std::string& v) {
     throw std::runtime_error("hunt profile must be general, mega, record60, or record80");
 }
 
+// HuntProfileConfig display names and gates (gpu_p20_benchmark.cpp:7262-7290).
 const char* profile_name(int p) {
-    static const char* names[] = {"GENERAL", "MEGA 30k+", "RECORD 60k+ (empirical)", "WORLD RECORD COARSE 700"};
+    static const char* names[] = {"GENERAL", "MEGA 30k+", "RECORD 60k+ (empirical)",
+                                  "WORLD RECORD COARSE 700 (compact-thick safe)"};
     return names[p];
+}
+
+struct Gates {
+    int p20, upper, high, coarse;
+    double p19;
+    bool megaTopology;
+};
+Gates profile_gates(int p) {
+    switch (p) {
+        case BSF_PROFILE_MEGA: return Gates{1, 8, 6, 85, 4.02, true};
+        case BSF_PROFILE_RECORD60: return Gates{3, 19, 12, 95, 6.70, false};
+        case BSF_PROFILE_RECORD80: return Gates{3, 19, 20, 700, 6.70, false};
+        default: return Gates{1, 5, 5, 85, 4.02, false};
+    }
+}
+
+// The stage pass counters of the stage0stream close summary, counted from the
+// response records as the reference counts them (gpu_p20_benchmark.cpp:7556-7571).
+struct StreamCounters {
+    unsigned long long p20 = 0, stage1 = 0, stage05 = 0, p19Evaluated = 0, p19Passed = 0, p19Rejected = 0,
+                       megaRejected = 0, coarseEvaluated = 0, coarsePassed = 0;
+
+    void add(const unsigned char* r, const Gates& g) {
+        const int a = r[0], b = r[1], c = r[2];
+        const int d = r[4] | (r[5] << 8);
+        if (a >= g.p20) ++p20;
+        if (a >= g.p20 && b >= g.upper) ++stage1;
+        if (a >= g.p20 && b >= g.upper && c >= g.high) {
+            ++stage05;
+            ++p19Evaluated;
+            if (r[3] != 0) {
+                ++p19Passed;
+                if (r[7] != 0) {
+                    ++megaRejected;
+                } else {
+                    ++coarseEvaluated;
+                    if (d >= g.coarse) ++coarsePassed;
+                }
+            } else {
+                ++p19Rejected;
+            }
+        }
+    }
+};
+
+// printDevice (gpu_p20_benchmark.cpp:979-992): the device lines of the startup banner.
+void print_device(int device) {
+    char info[512];
+    if (bsf_device_summary(device, info, sizeof(info)) == BSF_OK) std::fputs(info, stderr);
 }
 
 struct Handle {
@@ -106,17 +157,29 @@ int stage0stream(std::uint32_t capacity, int profile, bool research, int centers
     cfg.centers = centers;
     cfg.max_exact_radius = 1;
     Handle h(cfg);
+    const Gates g = profile_gates(profile);
+    // startup banner (gpu_p20_benchmark.cpp:7328-7343), logged verbatim by the app
+    print_device(cfg.device);
     std::fprintf(stderr, "Stage0+P19+coarse stream capacity: %u worlds / %llu regions\n", capacity,
                  static_cast<unsigned long long>(capacity) * centers);
-    std::fprintf(stderr, "GB300 worker profile: %s | fused P20/Upper/Lower/P19 kernel, device-queued coarse\n",
-                 profile_name(profile));
+    std::fprintf(stderr, "Production multi-center: %d exact radius-7 regions/world | 15-chunk spacing | "
+                 "region budget semantics\n", centers);
+    std::fprintf(stderr, "Profile: %s | P20>=%d | Upper>=%d | High>=%d | P19>=%g/extreme | Coarse>=%d | %s\n",
+                 profile_name(profile), g.p20, g.upper, g.high, g.p19, g.coarse,
+                 g.megaTopology ? "Mega topology reject ON" : "topology reject OFF");
+    if (profile == BSF_PROFILE_RECORD60 || profile == BSF_PROFILE_RECORD80)
+        std::fprintf(stderr, "WARNING: record profile is empirically validated, not mathematically lossless.\n");
     std::fprintf(stderr, "Response telemetry: %s\n",
                  research ? "RESEARCH 34 bytes/region" : "LEAN 16 bytes/region + exact P19 double");
+    std::fprintf(stderr, "Stage0+P19+coarse pipeline: exact P20 -> full upper survivors -> lower reentry -> "
+                 "exact Stage0.75 gate -> optional Mega topology reject -> exact radius-7 coarse score "
+                 "(GB300: FP32-screened kernels with exact FP64 fallback, device-side queues)\n");
     const std::size_t rec = research ? 34 : 16;
     const char magic[8] = {'S', 'T', '0', 'R', '3', '8', '1', '6'};
     if (!write_all(magic, 8)) return 0;
     std::vector<unsigned char> out;
     unsigned long long worlds = 0;
+    StreamCounters sc;
     for (;;) {
         std::uint32_t count = 0;
         bool eof = false;
@@ -130,14 +193,20 @@ int stage0stream(std::uint32_t capacity, int profile, bool research, int centers
         out[3] = static_cast<unsigned char>(count >> 24);
         const int st = bsf_stage0_filter(h.h, seeds.data(), count, out.data() + 4, out.size() - 4);
         if (st != BSF_OK) throw std::runtime_error(bsf_last_error(h.h));
+        for (std::size_t i = 0; i < static_cast<std::size_t>(count) * centers; ++i) sc.add(out.data() + 4 + i * rec, g);
         if (!write_all(out.data(), out.size())) {
             std::fprintf(stderr, "Stage0+P19+coarse stream parent closed response pipe; exiting cleanly\n");
             break;
         }
         worlds += count;
     }
-    std::fprintf(stderr, "Stage0+P19+coarse stream closed | worlds=%llu | regions=%llu\n", worlds,
-                 worlds * static_cast<unsigned long long>(centers));
+    // close summary (gpu_p20_benchmark.cpp:7601-7611)
+    std::fprintf(stderr,
+                 "Stage0+P19+coarse stream closed | worlds=%llu | regions=%llu | P20Passed=%llu | Stage1Passed=%llu"
+                 " | Stage0.5Passed=%llu | Stage0.75Evaluated=%llu | Stage0.75Passed=%llu | Stage0.75Rejected=%llu"
+                 " | MegaTopologyRejected=%llu | CoarseEvaluated=%llu | CoarsePassedTarget=%llu\n",
+                 worlds, worlds * static_cast<unsigned long long>(centers), sc.p20, sc.stage1, sc.stage05,
+                 sc.p19Evaluated, sc.p19Passed, sc.p19Rejected, sc.megaRejected, sc.coarseEvaluated, sc.coarsePassed);
     return 0;
 }
 

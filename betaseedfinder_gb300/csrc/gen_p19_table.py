@@ -9,13 +9,12 @@ and feature ids verbatim (as C hexadecimal double literals, so no decimal
 round trip can change a bit). The generated file is committed; the script is
 only rerun when the reference model changes.
 
-Usage: python gen_p19_table.py [path/to/p19_monster_gate.hpp]
+Usage: python gen_p19_table.py <path/to/native/src/p19_monster_gate.hpp>
 """
 import os
 import re
 import sys
 
-DEFAULT_SRC = "/root/reference/native/src/p19_monster_gate.hpp"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "p19_table.inc")
 
 # Feature expressions exactly as they appear in the reference trees. The id is
@@ -112,7 +111,9 @@ def build(toks):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_SRC
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_p19_table.py <path/to/native/src/p19_monster_gate.hpp>")
+    src = sys.argv[1]
     text = open(src).read()
     m = re.search(r"THRESHOLD = ([0-9.]+);", text)
     threshold = float(m.group(1))

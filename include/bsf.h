@@ -171,6 +171,11 @@ int bsf_mega_search_device(void* h, const int64_t* d_seeds, uint32_t count, int3
  * world-major, centre-minor), e.g. to sample rejected regions for exact audits. */
 int bsf_last_region_records(void* h, uint8_t* out, size_t out_len);
 
+/* The device lines of the worker's startup banner (printDevice,
+ * gpu_p20_benchmark.cpp:979-992): "GPU: <name>", "Architecture: sm_XY",
+ * "Compute units: N", "Global memory: G GiB", one per line, into out. */
+int bsf_device_summary(int32_t device, char* out, size_t out_len);
+
 /* Number of GPU kernel launches issued by the handle so far (instrumentation). */
 uint64_t bsf_kernel_launches(const void* h);
 

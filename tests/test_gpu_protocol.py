@@ -41,6 +41,25 @@ def test_stage0stream_batches_match_the_oracle():
         want = po.stage0_batch(seeds, centers=8, profile=1, research=True)
         assert np.array_equal(got, want.reshape(-1))
     assert pos == len(out)
+    # the close summary carries the reference's stage counters (gpu_p20_benchmark.cpp:7601-7611),
+    # here recounted from the oracle's records with the MEGA gates (P20 1, Upper 8, High 6, coarse 85)
+    recs = np.concatenate([po.stage0_batch(b, centers=8, profile=1, research=True).reshape(-1, 34) for b in batches])
+    a, b_, c = recs[:, 0].astype(int), recs[:, 1].astype(int), recs[:, 2].astype(int)
+    d = recs[:, 4].astype(int) | (recs[:, 5].astype(int) << 8)
+    s05 = (a >= 1) & (b_ >= 8) & (c >= 6)
+    p19 = s05 & (recs[:, 3] != 0)
+    mega = p19 & (recs[:, 7] != 0)
+    want = {"worlds": sum(len(x) for x in batches), "regions": 8 * sum(len(x) for x in batches),
+            "P20Passed": int((a >= 1).sum()), "Stage1Passed": int(((a >= 1) & (b_ >= 8)).sum()),
+            "Stage0.5Passed": int(s05.sum()), "Stage0.75Evaluated": int(s05.sum()),
+            "Stage0.75Passed": int(p19.sum()), "Stage0.75Rejected": int((s05 & ~p19).sum()),
+            "MegaTopologyRejected": int(mega.sum()), "CoarseEvaluated": int((p19 & ~mega).sum()),
+            "CoarsePassedTarget": int((p19 & ~mega & (d >= 85)).sum())}
+    line = [ln for ln in r.stderr.decode().splitlines() if ln.startswith("Stage0+P19+coarse stream closed")]
+    assert len(line) == 1, r.stderr.decode()
+    got = dict(f.strip().split("=") for f in line[0].split("|")[1:])
+    assert {k: int(v) for k, v in got.items()} == want
+    assert "Profile: MEGA 30k+ | P20>=1 | Upper>=8 | High>=6 | P19>=4.02/extreme | Coarse>=85" in r.stderr.decode()
 
 
 def test_stage0stream_rejects_oversized_and_truncated_batches():
