@@ -40,7 +40,8 @@ struct CoarseSmem {
     std::uint8_t xi[NOCT][HALF_ROWS], zi[NOCT][SIDE];
     float shape[HALF_COLS][4];  // screened column shapes (d5, its bound, d7, its bound; bound < 0: undecided)
     std::uint32_t mask[HALF_COLS];
-    int cursor, screened, fallbacks;
+    std::uint16_t climate[HALF_COLS];  // columns whose d5 needs the climate and noise4
+    int cursor, screened, fallbacks, climateCount;
 };
 
 __device__ __forceinline__ GenTable gtab(const CoarseSmem& s) {
@@ -76,10 +77,13 @@ __device__ __noinline__ unsigned exact_column_w(const CoarseSmem& s, int cx, int
 }
 
 
-// Column shape (climate at block 4c+2 + noise4/5) in FP32 with bounds; kx is the half-local row.
-// noise5 first: in the d6 < 0 branch d5 is 0.5 whatever the climate and noise4,
-// which are left out when every converged lane of the warp is in that branch.
-__device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
+// Column shape (BetaTerrain173.java:739-804) in FP32 with bounds, in two
+// passes; kx is the half-local row. The first takes noise5 and the d6/d7 half
+// (shape_d7_f) of every column and reports whether d5 needs the climate: in the
+// reference's d6 < 0 branch d5 is 0.5 whatever the climate and noise4 are. The
+// second pass computes them for the compacted list of the other columns only,
+// so the climate's simplex octaves run on full warps.
+__device__ __noinline__ bool coarse_shape_first(const CoarseSmem& s, int kx, int kz, float* sh) {
     float n5 = 0.0f;
 #pragma unroll 1  // rolled: the unrolled octaves overflow the instruction cache
     for (int o = 0; o < 16; ++o) {
@@ -87,28 +91,29 @@ __device__ __noinline__ void coarse_shape(const CoarseSmem& s, int cx, int cz, i
                         static_cast<float>(1 << o);
         n5 = o == 0 ? v : n5 + v;
     }
-    Fe d5{0.5f, 0.0f}, d7{0.0f, 0.0f};
+    Fe d7{0.0f, 0.0f};
     bool zeroD5 = false;
-    const bool decided = shape_d7_f(Fe{n5, E_N5}, d7, zeroD5);
-    zeroD5 = zeroD5 && decided;
-    if (!__all_sync(__activemask(), zeroD5)) {
-        Fe temp, rain;
-        climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
-        float n4 = 0.0f;
-#pragma unroll 1
-        for (int o = 0; o < 10; ++o) {
-            const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx),
-                                     ax_z(s, ST_N4 + o, kz)) * static_cast<float>(1 << o);
-            n4 = o == 0 ? v : n4 + v;
-        }
-        const Fe d5c = shape_d5_f(temp, rain, Fe{n4, E_N4});
-        d5 = zeroD5 ? Fe{0.5f, 0.0f} : d5c;
-    }
-    if (!decided) {
+    if (!shape_d7_f(Fe{n5, E_N5}, d7, zeroD5)) {
         sh[0] = 0.0f; sh[1] = -1.0f; sh[2] = 0.0f; sh[3] = 0.0f;
-        return;
+        return false;
     }
-    sh[0] = d5.v; sh[1] = d5.e; sh[2] = d7.v; sh[3] = d7.e;
+    sh[0] = 0.5f; sh[1] = 0.0f; sh[2] = d7.v; sh[3] = d7.e;
+    return !zeroD5;
+}
+
+__device__ __noinline__ void coarse_shape_climate(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
+    Fe temp, rain;
+    climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
+    float n4 = 0.0f;
+#pragma unroll 1
+    for (int o = 0; o < 10; ++o) {
+        const float v = octave2f(s.perm + (ST_N4 + o) * PERM_BYTES, ax_x(s, ST_N4 + o, kx),
+                                 ax_z(s, ST_N4 + o, kz)) * static_cast<float>(1 << o);
+        n4 = o == 0 ? v : n4 + v;
+    }
+    const Fe d5 = shape_d5_f(temp, rain, Fe{n4, E_N4});
+    sh[0] = d5.v;
+    sh[1] = d5.e;
 }
 
 template <int Y0, int N>
@@ -131,7 +136,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
     CoarseSmem& s = *reinterpret_cast<CoarseSmem*>(smem_raw);
     const int tid = threadIdx.x;
     const int jobs = min(*count, maxCount);
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.climateCount = 0; }
     for (int item = blockIdx.x; item < jobs * 2; item += gridDim.x) {
         const int job = item >> 1, half = item & 1;
         const RegionRef ref = queue[job];
@@ -179,13 +184,32 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
         // stops once its signs are certain, so costs vary, and a fixed split
         // would leave the CTA waiting for its slowest warp at every barrier.
         const int cols = rows * SIDE;
-        for (int g = tid; g < cols; g += CT) {
-            const int kx = g / SIDE, kz = g % SIDE;
-            coarse_shape(s, originX + row0 + kx, originZ + kz, kx, kz, s.shape[g]);
-            s.mask[g] = 0;
+        const int lane0 = tid & 31;
+        for (int base = 0; base < cols; base += CT) {
+            const int g = base + tid;
+            bool need = false;
+            if (g < cols) {
+                need = coarse_shape_first(s, g / SIDE, g % SIDE, s.shape[g]);
+                s.mask[g] = 0;
+            }
+            const unsigned vote = __ballot_sync(0xffffffffu, need);
+            int slot = 0;
+            if (lane0 == 0 && vote) slot = atomicAdd(&s.climateCount, __popc(vote));
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (need) s.climate[slot + __popc(vote & ((1u << lane0) - 1u))] = static_cast<std::uint16_t>(g);
         }
         if (tid == 0) s.cursor = 0;
         __syncthreads();
+        {
+            const int m = s.climateCount;
+            for (int j = tid; j < m; j += CT) {
+                const int g = s.climate[j];
+                const int kx = g / SIDE, kz = g % SIDE;
+                coarse_shape_climate(s, originX + row0 + kx, originZ + kz, kx, kz, s.shape[g]);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) s.climateCount = 0;
         // chunk b: range b / chunks of columns (b % chunks) * 32 + lane. Range-major, so
         // the warps run one range's code at a time (three at once overflow the
         // instruction cache).

@@ -57,10 +57,16 @@ struct alignas(16) WorldSmem {
     int p20[8], upper[8], high[8], gate[8];
 };
 
+// Column shapes of one wave of a phase's tasks (bsf_screen.cuh column_shape_f
+// in two passes, see shape_wave).
+constexpr int SHAPE_CAP = 1536;
+
 struct FastSmem {
     WorldSmem w[PAIR];
     std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
-    int taskCount, screened, fallbacks;
+    float4 shape[SHAPE_CAP];              // d5, its bound, d7, its bound (d5 bound < 0: undecided)
+    std::uint16_t climate[SHAPE_CAP];     // wave tasks whose d5 needs the climate and noise4
+    int taskCount, screened, fallbacks, climateCount;
     int cursor[3];                        // next unclaimed task of the P20, Upper and Lower phases
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
@@ -96,25 +102,48 @@ __device__ __forceinline__ void column_coords(int c, int col, int& cx, int& cz, 
 }
 
 // ---- screened FP32 path ---------------------------------------------------
-// Column shape (climate + noise4/5); returns false when the d5 branch is undecided.
-__device__ __noinline__ bool screened_shape(const WorldSmem& s, int c, int col, Fe& d5, Fe& d7) {
+// Column shape (BetaTerrain173.java:739-804) in two passes. The first takes
+// noise5 and the d6/d7 half (shape_d7_f) of every task of a wave; in the
+// reference's d6 < 0 branch (about 70% of Stage0 columns) d5 is 0.5 whatever
+// the climate and noise4 are, so only the other columns go on to the second
+// pass, which the CTA's threads share densely: the climate's ten simplex
+// octaves are the most expensive part of a screened column.
+__device__ __noinline__ bool shape_first(const WorldSmem& s, int c, int col, float4& sh) {
+    int cx, cz, kx, kz;
+    column_coords(c, col, cx, cz, kx, kz);
+    float n5 = 0.0f;
+#pragma unroll 1
+    for (int o = 0; o < 16; ++o) {
+        const int st = ST_N5 + o;
+        n5 = n5 + octave2f(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz)) *
+                      static_cast<float>(1 << o);  // 0.0f + first term is exact
+    }
+    Fe d7;
+    bool zeroD5 = false;
+    if (!shape_d7_f(Fe{n5, E_N5}, d7, zeroD5)) {
+        sh = make_float4(0.0f, -1.0f, 0.0f, 0.0f);  // d5 branch undecided: the exact path decides
+        return false;
+    }
+    sh = make_float4(0.5f, 0.0f, d7.v, d7.e);
+    return !zeroD5;
+}
+
+// Second pass: the climate and noise4 part of d5 (shape_d5_f).
+__device__ __noinline__ void shape_climate(const WorldSmem& s, int c, int col, float4& sh) {
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     Fe temp, rain;
     climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
-    // noise4 octaves 0..9, then noise5 octaves 0..15, through one loop body (code size)
-    float n4 = 0.0f, n5 = 0.0f;
+    float n4 = 0.0f;
 #pragma unroll 1
-    for (int i = 0; i < 26; ++i) {
-        static_assert(ST_N5 == ST_N4 + 10, "noise5 states follow noise4's");
-        const int st = ST_N4 + i;
-        const int o = i < 10 ? i : i - 10;
-        const float v = octave2f(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz)) *
-                        static_cast<float>(1 << o);
-        if (i < 10) n4 = n4 + v;  // 0.0f + first term is exact
-        else n5 = n5 + v;
+    for (int o = 0; o < 10; ++o) {
+        const int st = ST_N4 + o;
+        n4 = n4 + octave2f(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz)) *
+                      static_cast<float>(1 << o);
     }
-    return column_shape_f(temp, rain, Fe{n4, E_N4}, Fe{n5, E_N5}, d5, d7);
+    const Fe d5 = shape_d5_f(temp, rain, Fe{n4, E_N4});
+    sh.x = d5.v;
+    sh.y = d5.e;
 }
 
 // Screened signs of one column's levels [Y0, Y0+N) given its shape; false
@@ -150,14 +179,13 @@ __device__ __forceinline__ std::uint32_t fallback_entry(FastSmem& s, int q, int 
 }
 
 // P20 / Upper column task of world slot q: levels 11..15 (16 is air).
-__device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+__device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int c, int col, const float4& sh, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 1);
-    Fe d5, d7;
     unsigned bits = 0;
     Pending p;
-    if (!forceExact && screened_shape(w, c, col, d5, d7) &&
-        screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, d5, d7, bits)) {
+    if (!forceExact && sh.y >= 0.0f &&
+        screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, Fe{sh.x, sh.y}, Fe{sh.z, sh.w}, bits)) {
         w.mask17[c][col] = bits;
         return p;
     }
@@ -166,11 +194,11 @@ __device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int c, int col
 }
 
 // Lower column task: levels 0..5 and 6..10 (two screened tasks) on one shape.
-__device__ __forceinline__ Pending lower_task(FastSmem& s, int q, int c, int col, bool forceExact) {
+__device__ __forceinline__ Pending lower_task(FastSmem& s, int q, int c, int col, const float4& sh, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 2);
-    Fe d5, d7;
-    const bool shaped = !forceExact && screened_shape(w, c, col, d5, d7);
+    const bool shaped = !forceExact && sh.y >= 0.0f;
+    const Fe d5{sh.x, sh.y}, d7{sh.z, sh.w};
     unsigned lo = 0, hi = 0;
     const bool okLo = shaped && screened_range<0, 6>(w, c, col, d5, d7, lo);
     const bool okHi = shaped && screened_range<6, 5>(w, c, col, d5, d7, hi);
@@ -223,6 +251,42 @@ __device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body)
     __syncthreads();
 }
 
+// Shapes of wave tasks [t0, t0 + n), n <= SHAPE_CAP, into s.shape[0, n): the
+// first pass over every task, the climate pass over the compacted list of tasks
+// that need it, each spread over all threads; a barrier after each. coord(t)
+// gives a task's (slot, centre, column). Resets the phase's task cursor k.
+template <int FT, typename C>
+__device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bool forceExact, C coord) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid == 0) s.cursor[k] = 0;
+    if (!forceExact) {
+        for (int base = 0; base < n; base += FT) {
+            const int i = base + tid;
+            bool need = false;
+            if (i < n) {
+                int q, c, col;
+                coord(t0 + i, q, c, col);
+                need = shape_first(s.w[q], c, col, s.shape[i]);
+            }
+            const unsigned vote = __ballot_sync(0xffffffffu, need);
+            int slot = 0;
+            if (lane == 0 && vote) slot = atomicAdd(&s.climateCount, __popc(vote));
+            slot = __shfl_sync(0xffffffffu, slot, 0);
+            if (need) s.climate[slot + __popc(vote & ((1u << lane) - 1u))] = static_cast<std::uint16_t>(i);
+        }
+    }
+    __syncthreads();
+    const int m = s.climateCount;
+    for (int j = tid; j < m; j += FT) {
+        const int i = s.climate[j];
+        int q, c, col;
+        coord(t0 + i, q, c, col);
+        shape_climate(s.w[q], c, col, s.shape[i]);
+    }
+    __syncthreads();
+    if (tid == 0) s.climateCount = 0;
+}
+
 __device__ __forceinline__ int highest_reentry(std::uint32_t mask) {
     // stage0gpu::highestReentryYIndex (stage0_exact_gpu.hpp:552-566)
     bool sawPos = false, sawGap = false;
@@ -246,7 +310,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastSmem& s = *reinterpret_cast<FastSmem*>(smem_raw);
     const int tid = threadIdx.x;
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.climateCount = 0; }
     for (int pair = blockIdx.x; pair * PAIR < n; pair += gridDim.x) {
         const int w0 = pair * PAIR;
         const int nw = min(PAIR, n - w0);
@@ -294,11 +358,21 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
 
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         const int p20Tasks = centers * 64;
-        run_phase(s, 0, nw * p20Tasks, [&](int t) {
-            const int q = t / p20Tasks, u = t % p20Tasks;
-            const int c = u >> 6, k = u & 63;
-            return upper_task(s, q, c, cf_axis[k >> 3] * 16 + cf_axis[k & 7], fs.forceExact);
-        });
+        auto p20Coord = [&](int t, int& q, int& c, int& col) {
+            q = t / p20Tasks;
+            const int u = t % p20Tasks, k = u & 63;
+            c = u >> 6;
+            col = cf_axis[k >> 3] * 16 + cf_axis[k & 7];
+        };
+        for (int t0 = 0; t0 < nw * p20Tasks; t0 += SHAPE_CAP) {
+            const int wn = min(SHAPE_CAP, nw * p20Tasks - t0);
+            shape_wave<FT>(s, 0, t0, wn, fs.forceExact, p20Coord);
+            run_phase(s, 0, wn, [&](int i) {
+                int q, c, col;
+                p20Coord(t0 + i, q, c, col);
+                return upper_task(s, q, c, col, s.shape[i], fs.forceExact);
+            });
+        }
         for (int t = tid; t < nw * p20Tasks; t += FT) {
             const int q = t / p20Tasks, u = t % p20Tasks;
             const int c = u >> 6, k = u & 63;
@@ -321,10 +395,22 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
         const int upperUnits = s.taskCount;
-        run_phase(s, 1, upperUnits * 192, [&](int t) {
+        auto upperCoord = [&](int t, int& q, int& c, int& col) {
             const int e = s.tasks[t / 192];
-            return upper_task(s, e >> 3, e & 7, cf_nonaxis_cols[t % 192], fs.forceExact);
-        });
+            q = e >> 3;
+            c = e & 7;
+            col = cf_nonaxis_cols[t % 192];
+        };
+        for (int t0 = 0; t0 < upperUnits * 192; t0 += SHAPE_CAP) {
+            const int wn = min(SHAPE_CAP, upperUnits * 192 - t0);
+            shape_wave<FT>(s, 1, t0, wn, fs.forceExact, upperCoord);
+            run_phase(s, 1, wn, [&](int i) {
+                int q, c, col;
+                upperCoord(t0 + i, q, c, col);
+                return upper_task(s, q, c, col, s.shape[i], fs.forceExact);
+            });
+        }
+        __syncthreads();
         for (int t = tid; t < upperUnits * 192; t += FT) {
             const int e = s.tasks[t / 192];
             if (s.w[e >> 3].mask17[e & 7][cf_nonaxis_cols[t % 192]]) atomicAdd(&s.w[e >> 3].upper[e & 7], 1);
@@ -345,10 +431,23 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         __syncthreads();
         // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239)
         // that share the column's shape.
-        run_phase(s, 2, s.taskCount, [&](int i) {
-            const int e = s.tasks[i];
-            return lower_task(s, e >> 11, (e >> 8) & 7, e & 255, fs.forceExact);
-        });
+        const int lowerN = s.taskCount;
+        auto lowerCoord = [&](int t, int& q, int& c, int& col) {
+            const int e = s.tasks[t];
+            q = e >> 11;
+            c = (e >> 8) & 7;
+            col = e & 255;
+        };
+        for (int t0 = 0; t0 < lowerN; t0 += SHAPE_CAP) {
+            const int wn = min(SHAPE_CAP, lowerN - t0);
+            shape_wave<FT>(s, 2, t0, wn, fs.forceExact, lowerCoord);
+            run_phase(s, 2, wn, [&](int i) {
+                int q, c, col;
+                lowerCoord(t0 + i, q, c, col);
+                return lower_task(s, q, c, col, s.shape[i], fs.forceExact);
+            });
+        }
+        __syncthreads();
         // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
         for (int k = tid; k < nw * 8 * 256; k += FT)
             reinterpret_cast<std::uint8_t*>(&s.w[k >> 11].axf[0][0][0])[k & 2047] = 0xFF;
