@@ -204,38 +204,42 @@ constexpr float OCTAVE3_ABS_MAX = 1.55f;
 // Simplex sample with exact FP64 lattice geometry and an FP32 kernel: the
 // offsets d11..d16 are FP64 (they cancel large coordinates), the falloff and
 // gradients are FP32 tracked with bounds. Returns 70*(n0+n1+n2) with its bound.
+// One simplex corner, n = t^4 * (g . (x, z)) with t = 0.5 - x^2 - z^2 (0 when
+// t < 0), in FP32 with a first-order error bound (NoiseGenerator2173.java:
+// 111-174, simplexGrad2 :61-75). Inputs x, z lie within dx = u|x| + eg, dz =
+// u|z| + eg of the reference's FP64 offsets.
+//   t:  |t - t*| <= et = (2|x| + dx) dx + (2|z| + dz) dz + u (x^2 + z^2 + |c| + |t|),
+//       c = 0.5 - x^2, the four roundings of t's evaluation included;
+//   g:  the gradient picks (gx, gz) in {-1, 0, 1}^2, so d = gx x + gz z has
+//       |d - d*| <= egd = dx + dz + u |d|;
+//   n:  with tp = t + et >= max(t, t*): |t^4 - t*^4| <= 4 tp^3 et, so
+//       |n - n*| <= 4 tp^3 et (|d| + egd) + tp^4 egd + 4u tp^4 |d|, the last term
+//       for the roundings of t^2, t^4 and the product.
+// When |t| <= et the reference may or may not add the corner: it returns 0 and
+// adds the largest contribution, (|t| + et)^4 * 2, to the bound. Written without
+// branches on the gradient (lanes of a warp hold different corners).
 __device__ __forceinline__ float simplex_corner(float x, float z, int g, float& err, float eg = 0.0f) {
-    // x, z carry error <= u|.| + eg (rounded offsets, eg > 0 when they come from
-    // the double-float geometry below)
-    Fe X{x, fabsf(x) * U + eg}, Z{z, fabsf(z) * U + eg};
-    Fe t = fe_sub(fe_sub(Fe{0.5f, 0.0f}, fe_mul(X, X)), fe_mul(Z, Z));
-    if (fabsf(t.v) <= t.e) {
-        // the FP64 branch t < 0 may differ; the contribution is at most (|t|+e)^4 * 2
-        const float m = fabsf(t.v) + t.e;
-        err += m * m * m * m * 2.0f;
+    const float ax = fabsf(x), az = fabsf(z);
+    const float dx = ax * U + eg, dz = az * U + eg;
+    const float xx = x * x, zz = z * z;
+    const float c = 0.5f - xx;
+    const float t = c - zz;
+    const float et = (2.0f * ax + dx) * dx + (2.0f * az + dz) * dz + U * (xx + zz + fabsf(c) + fabsf(t));
+    // simplexGrad2: g 0..3 (+-x +-z), 4..7 (+-x), 8..11 (+-z)
+    const float gx = g < 8 ? ((g & 1) ? -1.0f : 1.0f) : 0.0f;
+    const float gz = g < 4 ? ((g & 2) ? -1.0f : 1.0f) : (g < 8 ? 0.0f : ((g & 1) ? -1.0f : 1.0f));
+    const float d = gx * x + gz * z;
+    const float ad = fabsf(d);
+    const float egd = dx + dz + U * ad;
+    const float tp = fabsf(t) + et;
+    const float tp2 = tp * tp, tp4 = tp2 * tp2;
+    if (t <= et) {  // t* < 0 (nothing added) or its sign is undecided
+        if (t >= -et) err += tp4 * 2.0f;
         return 0.0f;
     }
-    if (t.v < 0.0f) return 0.0f;
-    Fe gx, gz;
-    // simplexGrad2 (NoiseGenerator2173.java:61-75)
-    float gv;
-    switch (g) {
-        case 0: gv = x + z; gx = fe_add(X, Z); break;
-        case 1: gv = -x + z; gx = fe_sub(Z, X); break;
-        case 2: gv = x - z; gx = fe_sub(X, Z); break;
-        case 3: gv = -x - z; gx = fe_add(X, Z); gx.v = -gx.v; break;
-        case 4: case 6: gv = x; gx = X; break;
-        case 5: case 7: gv = -x; gx = Fe{-X.v, X.e}; break;
-        case 8: case 10: gv = z; gx = Z; break;
-        default: gv = -z; gx = Fe{-Z.v, Z.e}; break;
-    }
-    (void)gv;
-    (void)gz;
-    const Fe t2 = fe_mul(t, t);
-    const Fe t4 = fe_mul(t2, t2);
-    const Fe n = fe_mul(t4, gx);
-    err += n.e;
-    return n.v;
+    err += 4.0f * tp2 * tp * et * (ad + egd) + tp4 * (egd + 4.0f * U * ad);
+    const float t2 = t * t;
+    return (t2 * t2) * d;
 }
 
 // Out of line: the climate's ten octaves would otherwise inline ten copies.
