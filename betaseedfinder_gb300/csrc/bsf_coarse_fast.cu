@@ -41,6 +41,7 @@ struct CoarseSmem {
     float shape[HALF_COLS][4];  // screened column shapes (d5, its bound, d7, its bound; bound < 0: undecided)
     std::uint32_t mask[HALF_COLS];
     std::uint16_t climate[HALF_COLS];  // columns whose d5 needs the climate and noise4
+    float4 clim[10];                   // climate generators' offsets as float pairs (climate_split)
     int cursor, screened, fallbacks, climateCount;
 };
 
@@ -103,7 +104,7 @@ __device__ __noinline__ bool coarse_shape_first(const CoarseSmem& s, int kx, int
 
 __device__ __noinline__ void coarse_shape_climate(const CoarseSmem& s, int cx, int cz, int kx, int kz, float* sh) {
     Fe temp, rain;
-    climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
+    climate_f(gtab(s), s.clim, cx * 4 + 2, cz * 4 + 2, temp, rain);
     float n4 = 0.0f;
 #pragma unroll 1
     for (int o = 0; o < 10; ++o) {
@@ -162,6 +163,8 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             YEntry ya[17];
             build_yaxis(sy, s.off[o][1], ya);
             build_yf(ya, s.yf[o]);
+        } else if (tid < OCT3 + 10) {
+            s.clim[tid - OCT3] = climate_split(s.off[ST_TEMP + tid - OCT3]);
         }
         for (int e = tid; e < NOCT * (rows + SIDE); e += CT) {
             const int o = e / (rows + SIDE), k = e % (rows + SIDE);

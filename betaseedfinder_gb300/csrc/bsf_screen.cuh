@@ -344,10 +344,18 @@ __device__ __forceinline__ bool df_floor(DF v, int& out) {
     return fabsf(to_n) > SIMPLEX_EPS && fabsf(to_n1) > SIMPLEX_EPS;
 }
 
+// The ten climate generators' FP64 offsets a and b as float pairs (a.h, a.l,
+// b.h, b.l), split once per staged world: climate_split(off of state ST_TEMP + i).
+__device__ __forceinline__ float4 climate_split(const double* abc) {
+    const DF a = df_of(abc[0]), b = df_of(abc[1]);
+    return make_float4(a.h, a.l, b.h, b.l);
+}
+
 // simplex2f with the geometry in double-float (xs = X * sx, zs = Z * sx for the
-// integer block coordinates X, Z); false when a decision is too close to call,
-// in which case the caller takes the FP64 geometry.
-static __device__ __noinline__ bool simplex2f_df(const Gen& s, int bx, int bz, double sx, Fe& out) {
+// integer block coordinates X, Z; ab = climate_split of the generator); false
+// when a decision is too close to call, in which case the caller takes the FP64
+// geometry.
+static __device__ __noinline__ bool simplex2f_df(const Gen& s, float4 ab, int bx, int bz, double sx, Fe& out) {
     constexpr double F = 0.3660254037844386;
     constexpr double G = 0.21132486540518713;
     constexpr float FH = static_cast<float>(F), FL = static_cast<float>(F - static_cast<double>(FH));
@@ -356,8 +364,8 @@ static __device__ __noinline__ bool simplex2f_df(const Gen& s, int bx, int bz, d
     constexpr float G1H = static_cast<float>(G1), G1L = static_cast<float>(G1 - static_cast<double>(G1H));
     constexpr float G2H = static_cast<float>(G2), G2L = static_cast<float>(G2 - static_cast<double>(G2H));
     const DF sxd = df_of(sx);
-    const DF d5 = df_add(df_mul_f(static_cast<float>(bx), sxd), df_of(s.a));
-    const DF d6 = df_add(df_mul_f(static_cast<float>(bz), sxd), df_of(s.b));
+    const DF d5 = df_add(df_mul_f(static_cast<float>(bx), sxd), DF{ab.x, ab.y});
+    const DF d6 = df_add(df_mul_f(static_cast<float>(bz), sxd), DF{ab.z, ab.w});
     const DF d7 = df_mul(df_add(d5, d6), DF{FH, FL});
     int j1, k1;
     if (!df_floor(df_add(d5, d7), j1) || !df_floor(df_add(d6, d7), k1)) return false;
@@ -387,8 +395,10 @@ static __device__ __noinline__ bool simplex2f_df(const Gen& s, int bx, int bz, d
     return true;
 }
 
-// Climate (temperature, rain) with bounds (WorldChunkManager173.java:95-126).
-__device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe& temperature, Fe& rain) {
+// Climate (temperature, rain) with bounds (WorldChunkManager173.java:95-126);
+// clim[i] = climate_split of climate generator i.
+__device__ __forceinline__ void climate_f(const GenTable& t, const float4* clim, int bx, int bz, Fe& temperature,
+                                          Fe& rain) {
     const double X = static_cast<double>(bx);
     const double Z = static_cast<double>(bz);
     Fe raw[3];
@@ -409,7 +419,7 @@ __device__ __forceinline__ void climate_f(const GenTable& t, int bx, int bz, Fe&
                 const float w = static_cast<float>(0.55 / d6);  // 0.55 * 2^k: FP32 rounding of w tracked below
                 const Gen g = t(ST_TEMP + base[grp] + o);
                 Fe s;
-                if (!simplex2f_df(g, bx, bz, sx, s)) s = simplex2f(g, X * sx, Z * sx);
+                if (!simplex2f_df(g, clim[base[grp] + o], bx, bz, sx, s)) s = simplex2f(g, X * sx, Z * sx);
                 const Fe term{s.v * w, s.e * w + fabsf(s.v * w) * 2.0f * U};
                 acc = fe_add(acc, term);
                 d7 *= octScale[grp];

@@ -54,6 +54,7 @@ struct alignas(16) WorldSmem {
     float axd[NOCT][2][NAX];   // FP32 fade
     std::uint8_t axi[NOCT][2][NAX];  // lattice index & 255
     std::uint32_t mask17[8][256];
+    float4 clim[10];  // climate generators' offsets as float pairs (climate_split)
     int p20[8], upper[8], high[8], gate[8];
 };
 
@@ -133,7 +134,7 @@ __device__ __noinline__ void shape_climate(const WorldSmem& s, int c, int col, f
     int cx, cz, kx, kz;
     column_coords(c, col, cx, cz, kx, kz);
     Fe temp, rain;
-    climate_f(gtab(s), cx * 4 + 2, cz * 4 + 2, temp, rain);
+    climate_f(gtab(s), s.clim, cx * 4 + 2, cz * 4 + 2, temp, rain);
     float n4 = 0.0f;
 #pragma unroll 1
     for (int o = 0; o < 10; ++o) {
@@ -342,6 +343,9 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             YEntry ya[17];
             build_yaxis(sy, s.w[q].off[o][1], ya);
             build_yf(ya, s.w[q].yf[o]);
+        } else if (tid < OCT3 * nw + 10 * nw) {
+            const int q = (tid - OCT3 * nw) / 10, i = (tid - OCT3 * nw) % 10;
+            s.w[q].clim[i] = climate_split(s.w[q].off[ST_TEMP + i]);
         }
         constexpr int AXES = NOCT * 2 * NAX;
         for (int e = tid; e < nw * AXES; e += FT) {
