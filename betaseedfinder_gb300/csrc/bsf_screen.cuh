@@ -344,6 +344,43 @@ __device__ __forceinline__ bool df_floor(DF v, int& out) {
     return fabsf(to_n) > SIMPLEX_EPS && fabsf(to_n1) > SIMPLEX_EPS;
 }
 
+// Axis entry (as make_axis) from double-float inputs: `coord` an integer
+// lattice coordinate, sc the octave's FP64 scale and off the generator's FP64
+// offset, both split into float pairs. coord * sc + off (|.| < 2^17), its floor
+// and fraction and the fraction's fade are taken in double-float: within 2^-32
+// of the real values, and the reference's FP64 sum is within 2^-36 of its real
+// value. Rounded to FP32, the fraction and fade then carry u|x| plus at most
+// 2^-30 (the fade's slope is below 2) against the FP64 entry. That absolute
+// term moves a 3D octave value by under 10 * 2^-30 = 1e-8 (each input enters a
+// gradient or a lerp weight with a factor of at most 4, and the lerps are
+// convex), far inside the margin between E_OCT3 (2e-5) and the 1.43e-5 of its
+// derivation, and likewise for E_OCT2 (6e-6 against 4.6e-6). false when the
+// sum is within SIMPLEX_EPS of an integer: the FP64 floor decides that entry.
+__device__ __forceinline__ bool make_axis_df(int coord, DF sc, DF off, AxisF& a) {
+    const DF v = df_add(df_mul_f(static_cast<float>(coord), sc), off);
+    const float n = floorf(v.h);
+    const DF lo = two_sum(v.h, -n);
+    DF fr = fast_two_sum(lo.h, lo.l + v.l);  // v - n, exact to the pair's precision
+    float base = n;
+    if (fr.h < 0.0f) {
+        fr = df_add(fr, DF{1.0f, 0.0f});
+        base -= 1.0f;
+    } else if (fr.h >= 1.0f) {
+        fr = df_add(fr, DF{-1.0f, 0.0f});
+        base += 1.0f;
+    }
+    if (!(fr.h > SIMPLEX_EPS && fr.h < 1.0f - SIMPLEX_EPS)) return false;
+    a.i = static_cast<int>(base) & 255;
+    a.f = fr.h + fr.l;
+    a.f1 = a.f - 1.0f;
+    // fade = t^3 (t (6t - 15) + 10), the reference's expression
+    const DF inner = df_add(df_mul(fr, df_add(df_mul_f(6.0f, fr), DF{-15.0f, 0.0f})), DF{10.0f, 0.0f});
+    const DF t3 = df_mul(df_mul(fr, fr), fr);
+    const DF fd = df_mul(t3, inner);
+    a.fd = fd.h + fd.l;
+    return true;
+}
+
 // The ten climate generators' FP64 offsets a and b as float pairs (a.h, a.l,
 // b.h, b.l), split once per staged world: climate_split(off of state ST_TEMP + i).
 __device__ __forceinline__ float4 climate_split(const double* abc) {

@@ -22,6 +22,7 @@
 #include "bsf_internal.h"
 #include "bsf_screen.cuh"
 
+#include <cmath>
 #include <cstdio>
 #include <stdexcept>
 
@@ -38,6 +39,7 @@ constexpr int NOCT = 66;      // 40 3D + 26 2D lattice octaves (state index == o
 constexpr int PAIR = 2;        // worlds staged per CTA pass (measured: 9% faster than one)
 
 __constant__ unsigned char cf_axis[8] = {0, 2, 5, 7, 8, 10, 13, 15};
+__constant__ float2 cf_octave_scale[66];  // octave_scale(o) split into a float pair
 __constant__ unsigned char cf_nonaxis_cols[192];
 __constant__ signed char cf_p19_feature[BSF_P19_NODE_COUNT];
 __constant__ short cf_p19_left[BSF_P19_NODE_COUNT];
@@ -322,7 +324,17 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             uint4* dst = reinterpret_cast<uint4*>(s.w[q].perm);
             for (int k = tid; k < WORLD_PERM_BYTES / 16; k += FT) dst[k] = src[k];
             const double* o = cache.offsets + static_cast<std::size_t>(w0 + q) * WORLD_OFFSETS;
-            for (int k = tid; k < ST_COUNT * 3; k += FT) s.w[q].off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
+            // the lattice octaves' X (a) and Z (c) offsets also go to the axis phase as float
+            // pairs, in the shape buffer, which the phases only use later
+            float2* split = reinterpret_cast<float2*>(s.shape) + q * NOCT * 2;
+            for (int k = tid; k < ST_COUNT * 3; k += FT) {
+                const double v = o[(k / 3) * 4 + (k % 3)];
+                s.w[q].off[k / 3][k % 3] = v;
+                if (k / 3 < NOCT && k % 3 != 1) {
+                    const DF d = df_of(v);
+                    split[(k / 3) * 2 + (k % 3) / 2] = make_float2(d.h, d.l);
+                }
+            }
         }
         if (tid < 8 * nw) {
             WorldSmem& w = s.w[tid >> 3];
@@ -347,13 +359,19 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             const int q = (tid - OCT3 * nw) / 10, i = (tid - OCT3 * nw) % 10;
             s.w[q].clim[i] = climate_split(s.w[q].off[ST_TEMP + i]);
         }
-        constexpr int AXES = NOCT * 2 * NAX;
-        for (int e = tid; e < nw * AXES; e += FT) {
-            WorldSmem& w = s.w[e / AXES];
-            const int f = e % AXES;
-            const int o = f / (2 * NAX), a = (f / NAX) & 1, k = f % NAX;
-            const double coord = static_cast<double>(-88 + 4 * k);
-            const AxisF ax = make_axis(coord * octave_scale(o), w.off[o][a == 0 ? 0 : 2]);
+        // Axis table entries in double-float (FP64 only where a floor is too close to
+        // call). One centre reads coordinates 15..30 only (kx = ix + 15).
+        const int nk = centers == 1 ? 16 : NAX, k0 = centers == 1 ? 15 : 0;
+        const int axes = NOCT * 2 * nk;
+        for (int e = tid; e < nw * axes; e += FT) {
+            const int q = e / axes, f = e % axes;
+            WorldSmem& w = s.w[q];
+            const int o = f / (2 * nk), a = (f / nk) & 1, k = k0 + f % nk;
+            const float2 sc = cf_octave_scale[o];
+            const float2 of = reinterpret_cast<const float2*>(s.shape)[(q * NOCT + o) * 2 + a];
+            AxisF ax;
+            if (!make_axis_df(-88 + 4 * k, DF{sc.x, sc.y}, DF{of.x, of.y}, ax))
+                ax = make_axis(static_cast<double>(-88 + 4 * k) * octave_scale(o), w.off[o][a == 0 ? 0 : 2]);
             w.axf[o][a][k] = ax.f;
             w.axd[o][a][k] = ax.fd;
             w.axi[o][a][k] = static_cast<std::uint8_t>(ax.i);
@@ -678,7 +696,23 @@ const char* stage0_fast_variant_name(int v) { return g_variants[v].name; }
 void set_stage0_fast_variant(int v) { g_variant = (v >= 0 && v < kVariants) ? v : 0; }
 int get_stage0_fast_variant() { return g_variant; }
 
+// octave_scale(o) on the host, in the same IEEE operations as the device.
+double octave_scale_host(int o) {
+    if (o < 16) return NOISE_XZ * std::ldexp(1.0, -o);
+    if (o < 32) return NOISE_XZ * std::ldexp(1.0, -(o - 16));
+    if (o < 40) return (NOISE_XZ / 80.0) * std::ldexp(1.0, -(o - 32));
+    if (o < 50) return 1.121 * std::ldexp(1.0, -(o - 40));
+    return 200.0 * std::ldexp(1.0, -(o - 50));
+}
+
 void init_stage0_fast() {
+    float2 scales[NOCT];
+    for (int o = 0; o < NOCT; ++o) {
+        const double v = octave_scale_host(o);
+        const float h = static_cast<float>(v);
+        scales[o] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+    }
+    check(cudaMemcpyToSymbol(cf_octave_scale, scales, sizeof(scales)), "octave scales");
     check(cudaMemcpyToSymbol(cf_p19_feature, bsf_p19_feature, sizeof(bsf_p19_feature)), "p19");
     check(cudaMemcpyToSymbol(cf_p19_left, bsf_p19_left, sizeof(bsf_p19_left)), "p19");
     check(cudaMemcpyToSymbol(cf_p19_right, bsf_p19_right, sizeof(bsf_p19_right)), "p19");
