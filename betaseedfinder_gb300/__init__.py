@@ -118,7 +118,7 @@ PENDING = 1
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_stage0_sweep", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
-           "bsf_kernel_launches", "bsf_device_summary", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
+           "bsf_kernel_launches", "bsf_device_summary", "bsf_screen_probe", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
            "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_last_region_records", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
            "bsf_server_last_error", "bsf_server_submit_range", "bsf_server_submit_preview", "bsf_server_poll",
@@ -191,6 +191,26 @@ def load(path=LIB_PATH):
     L.bsf_server_get_stats.argtypes = [vp, P(ServerStats)]
     _lib = L
     return L
+
+
+PROBE_KINDS = ("octave3_fp64_axes", "octave3_df_axes", "octave2_fp64_axes", "octave2_df_axes",
+               "simplex_df_geometry", "simplex_fp64_geometry", "climate", "column_shape")
+
+
+def screen_probe(seeds, samples_per_thread=32, rng=1):
+    """Largest |FP32 - FP64| / bound per screening primitive (bsf_screen_probe)."""
+    L = load()
+    seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+    ratio = (ctypes.c_double * len(PROBE_KINDS))()
+    counts = (ctypes.c_uint64 * len(PROBE_KINDS))()
+    err = ctypes.create_string_buffer(256)
+    L.bsf_screen_probe.argtypes = [ctypes.POINTER(ctypes.c_int64), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p,
+                                   ctypes.c_size_t]
+    st = L.bsf_screen_probe(_p(seeds, ctypes.c_int64), len(seeds), samples_per_thread, rng, ratio, counts, err, 256)
+    if st != 0:
+        raise BsfError("bsf_screen_probe: %s" % err.value.decode())
+    return {k: (ratio[i], counts[i]) for i, k in enumerate(PROBE_KINDS)}
 
 
 def measure_peaks():

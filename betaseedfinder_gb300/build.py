@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
 CU_SOURCES = ["bsf_stage0.cu", "bsf_stage0_fast.cu", "bsf_coarse.cu", "bsf_coarse_fast.cu", "bsf_exact.cu",
-              "bsf_sweep.cu", "bsf_api.cu", "bsf_noalloc.cu", "bsf_server.cu"]
+              "bsf_sweep.cu", "bsf_probe.cu", "bsf_api.cu", "bsf_noalloc.cu", "bsf_server.cu"]
 LIB = os.path.join(BUILD, "libbsf.so")
 WORKER = os.path.join(BUILD, "bsf_worker")
 

@@ -218,13 +218,19 @@ constexpr float OCTAVE3_ABS_MAX = 1.55f;
 // When |t| <= et the reference may or may not add the corner: it returns 0 and
 // adds the largest contribution, (|t| + et)^4 * 2, to the bound. Written without
 // branches on the gradient (lanes of a warp hold different corners).
+// The first-order terms leave out products of errors, and measured errors came
+// within 0.74 of them (bsf_screen_probe), so et and the returned term are taken
+// twice: every tracked bound downstream (climate, column shape) then keeps a
+// margin of two over its measured error, and the intermediate branch decisions
+// that use a bound undoubled (the corner sign here, the d6 branch, the noise
+// selector) inherit it.
 __device__ __forceinline__ float simplex_corner(float x, float z, int g, float& err, float eg = 0.0f) {
     const float ax = fabsf(x), az = fabsf(z);
     const float dx = ax * U + eg, dz = az * U + eg;
     const float xx = x * x, zz = z * z;
     const float c = 0.5f - xx;
     const float t = c - zz;
-    const float et = (2.0f * ax + dx) * dx + (2.0f * az + dz) * dz + U * (xx + zz + fabsf(c) + fabsf(t));
+    const float et = 2.0f * ((2.0f * ax + dx) * dx + (2.0f * az + dz) * dz + U * (xx + zz + fabsf(c) + fabsf(t)));
     // simplexGrad2: g 0..3 (+-x +-z), 4..7 (+-x), 8..11 (+-z)
     const float gx = g < 8 ? ((g & 1) ? -1.0f : 1.0f) : 0.0f;
     const float gz = g < 4 ? ((g & 2) ? -1.0f : 1.0f) : (g < 8 ? 0.0f : ((g & 1) ? -1.0f : 1.0f));
@@ -237,7 +243,7 @@ __device__ __forceinline__ float simplex_corner(float x, float z, int g, float& 
         if (t >= -et) err += tp4 * 2.0f;
         return 0.0f;
     }
-    err += 4.0f * tp2 * tp * et * (ad + egd) + tp4 * (egd + 4.0f * U * ad);
+    err += 2.0f * (4.0f * tp2 * tp * et * (ad + egd) + tp4 * (egd + 4.0f * U * ad));
     const float t2 = t * t;
     return (t2 * t2) * d;
 }

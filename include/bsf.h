@@ -198,6 +198,20 @@ int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_vari
  * with CUDA events. ops_per_s[0] = FP64 DADD/s, ops_per_s[1] = FP32 FADD/s. */
 int bsf_measure_peaks(double* ops_per_s2);
 
+/* Screen-bound probe (instrumentation): for `worlds` seeds' real generator
+ * states, evaluates every FP32 screening primitive beside its exact FP64 twin at
+ * random lattice points (samples_per_thread samples in each of 77,824 threads)
+ * and writes, per kind, the largest |FP32 - FP64| divided by the bound the
+ * screen uses, and the samples taken. Kinds: 0/1 one 3D octave against
+ * E_OCT3 with FP64 / double-float axis entries, 2/3 one 2D octave against
+ * E_OCT2 (same), 4/5 one simplex sample against its tracked bound with
+ * double-float / FP64 lattice geometry, 6 temperature and rain, 7 column shape
+ * d5 and d7, against their tracked bounds. The screen is sound while every
+ * ratio stays below 1. Allocates its own device memory. */
+#define BSF_PROBE_KINDS 8
+int bsf_screen_probe(const int64_t* seeds, uint32_t worlds, uint32_t samples_per_thread, uint64_t rng,
+                     double* max_ratio, uint64_t* counts, char* err, size_t err_len);
+
 /* Switches the hunt profile (BSF_PROFILE_*) of later batch calls on this handle
  * (the worker argv profile, chosen per request instead of per process). */
 int bsf_set_profile(void* h, int32_t profile);
