@@ -716,9 +716,21 @@ def main():
         for s in range(args.plain_steps):  # untimed: the records of the same batches again, kept
             worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
             plain_regions.append(worker.last_region_records(B))
+        # the same stage-by-stage driving on the screened kernels: separates what the
+        # device queues and batch graphs add from what the FP32 screen adds
+        worker.set_mode(bsf.MODE_PLAIN_SCREENED)
+        worker.mega_search_device(d_seeds[0].data_ptr(), B, radius=args.radius, stream=sptr)  # warm-up
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        pscr_out = []
+        for s in range(args.plain_steps):
+            c, r = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+            pscr_out.append([(x.world_index, x.center_index, x.island.key()) for x in r])
+        torch.cuda.synchronize()
+        plain_screened = B * args.plain_steps / (time.perf_counter() - p0)
         worker.set_mode(bsf.MODE_QUEUED)
         mismatched_regions = 0
-        mismatched_batches = 0
+        mismatched_batches = sum(1 for s in range(args.plain_steps) if pscr_out[s] != plain_out[s][1])
         for s in range(args.plain_steps):
             c, r = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
             q = worker.last_region_records(B).reshape(-1, 34)
@@ -729,6 +741,9 @@ def main():
                 mismatched_batches += 1
         extras["forms"] = {"queued_worlds_per_s": value / dist.world, "plain_worlds_per_s": plain,
                            "queued_over_plain": (value / dist.world) / plain,
+                           "plain_screened_worlds_per_s": plain_screened,
+                           "queued_over_plain_screened": (value / dist.world) / plain_screened,
+                           "plain_screened_over_plain": plain_screened / plain,
                            "verified": {"worlds": B * args.plain_steps, "regions": B * 8 * args.plain_steps,
                                         "mismatched_region_records": mismatched_regions,
                                         "mismatched_batches": mismatched_batches,

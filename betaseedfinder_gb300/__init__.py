@@ -23,7 +23,7 @@ WORKER_PATH = os.path.join(HERE, "_build", "bsf_worker")
 
 PROFILE_GENERAL, PROFILE_MEGA, PROFILE_RECORD60, PROFILE_RECORD80 = 0, 1, 2, 3
 PROFILES = {"general": 0, "mega": 1, "record60": 2, "record80": 3}
-MODE_QUEUED, MODE_PLAIN = 0, 1
+MODE_QUEUED, MODE_PLAIN, MODE_PLAIN_SCREENED = 0, 1, 2
 CENTER_CHUNK_X = (0, 15, 0, 15, -15, -15, 0, 15)
 CENTER_CHUNK_Z = (0, 0, 15, 15, 0, 15, -15, -15)
 

@@ -109,6 +109,29 @@ __global__ void k_stage_counts(const RegionInfo* __restrict__ regions, int count
     }
 }
 
+// One exact-stage region with everything the host needs to resolve and report it.
+struct ExactItem {
+    RegionRef ref;
+    std::int64_t seed;
+    RegionInfo info;
+};
+static_assert(sizeof(ExactItem) == 64, "ExactItem layout");
+
+// Gathers the exact-stage queue's regions (outcome and world seed) into one
+// contiguous array, so the host reads them with one copy instead of one per region.
+__global__ void k_gather_exact(const RegionRef* __restrict__ queue, const int* count, int cap,
+                               const RegionInfo* __restrict__ regions, const std::int64_t* __restrict__ seeds,
+                               int centers, ExactItem* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*count, cap)) return;
+    const RegionRef r = queue[i];
+    ExactItem e;
+    e.ref = r;
+    e.seed = seeds[r.world];
+    e.info = regions[static_cast<std::size_t>(r.world) * centers + r.center];
+    out[i] = e;
+}
+
 // Issue-rate probes: 8 independent dependent-add chains per thread.
 template <typename T>
 __global__ void k_add_chains(T* out, int iters, T inc) {
@@ -135,6 +158,10 @@ static std::shared_mutex& capture_guard() {
     static std::shared_mutex m;
     return m;
 }
+
+// Exact-stage regions copied back inside every batch (a 32,768-world MEGA batch
+// has about 13); more cost one further copy.
+constexpr int kExactPrefix = 256;
 
 // One exact-scan context: a stream, exact-scan scratch and a result slot.
 // Context 0 is the handle's own (its stream, scratch and preview buffers); the
@@ -175,6 +202,8 @@ struct BsfHandle {
     std::uint64_t* dHashes = nullptr;
     unsigned long long* dStageCounts = nullptr;
     RegionRef* dExactQueue = nullptr;
+    ExactItem* dExactItems = nullptr;  // gathered exact-stage regions (k_gather_exact)
+    ExactItem* hExactItems = nullptr;  // pinned copy; the first kExactPrefix come back inside the batch
     void* dExactBase = nullptr;
     ExactScratch exact;
     Stage0FastScratch fs;
@@ -337,8 +366,50 @@ void run_gpu_stages_plain(BsfHandle* h, int n) {
                               h->stream),
               "coarse list upload");
         check(cudaMemcpyAsync(h->dCounters, &chunk, sizeof(int), cudaMemcpyHostToDevice, h->stream), "count");
-        launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, chunk, LatticeBuffers{}, h->dSigns, h->dLabels,
-                            h->dStats, h->dRegions, h->centers, h->stream);
+        // maxCount = the queue's capacity (the device-side count bounds the work): the
+        // score kernel's grid, and with it the place of its retry-bound flag, is then
+        // the one the batch resets and reads
+        launch_coarse_score(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, LatticeBuffers{}, h->dSigns,
+                            h->dLabels, h->dStats, h->dRegions, h->centers, h->stream);
+        h->launches += 2;
+        check(cudaStreamSynchronize(h->stream), "coarse micro-batch");
+    }
+}
+
+// Plain form on the screened kernels: the same FP32-screened Stage0 and coarse
+// kernels as the queued form, driven stage by stage like run_gpu_stages_plain
+// (region records downloaded, the coarse list built on the host and fed in
+// micro-batches of 1024 with a sync each). Against the queued form it isolates
+// what the device queues and batch graphs contribute; against the FP64 plain
+// form, what the screen contributes.
+void run_gpu_stages_plain_screened(BsfHandle* h, int n) {
+    check(cudaStreamSynchronize(h->stream), "world init");
+    check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
+    launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, nullptr, h->dCounters, 0, h->fs, h->stream,
+                       h->persistent);
+    h->launches += 2;
+    const int regions = n * h->centers;
+    h->hRegions.resize(regions);
+    check(cudaMemcpyAsync(h->hRegions.data(), h->dRegions, sizeof(RegionInfo) * regions, cudaMemcpyDeviceToHost,
+                          h->stream),
+          "region download");
+    check(cudaStreamSynchronize(h->stream), "stage0");
+    std::vector<RegionRef> list;
+    for (int i = 0; i < regions; ++i) {
+        const RegionInfo& r = h->hRegions[i];
+        if (r.p19Evaluated && r.p19Pass && !r.megaReject) list.push_back(RegionRef{i / h->centers, i % h->centers});
+    }
+    const int micro = std::min(1024, h->coarseCap);
+    for (std::size_t off = 0; off < list.size(); off += micro) {
+        const int chunk = static_cast<int>(std::min<std::size_t>(micro, list.size() - off));
+        check(cudaMemcpyAsync(h->dCoarseQueue, list.data() + off, sizeof(RegionRef) * chunk, cudaMemcpyHostToDevice,
+                              h->stream),
+              "coarse list upload");
+        check(cudaMemcpyAsync(h->dCounters, &chunk, sizeof(int), cudaMemcpyHostToDevice, h->stream), "count");
+        launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, chunk, h->dSigns, h->fs.stats, h->stream,
+                                 h->persistent, h->fs.forceExact != 0);
+        launch_coarse_cc(h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, h->dLabels, h->dStats, h->dRegions,
+                         h->centers, h->stream);  // maxCount: as in run_gpu_stages_plain
         h->launches += 2;
         check(cudaStreamSynchronize(h->stream), "coarse micro-batch");
     }
@@ -346,14 +417,16 @@ void run_gpu_stages_plain(BsfHandle* h, int n) {
 
 void run_gpu_stages(BsfHandle* h, int n) {
     if (h->mode == BSF_MODE_PLAIN) run_gpu_stages_plain(h, n);
+    else if (h->mode == BSF_MODE_PLAIN_SCREENED) run_gpu_stages_plain_screened(h, n);
     else run_gpu_stages_queued(h, n);
 }
 
 // Stage0 and coarse bracketed by events (event 2 sits between them in the
-// queued form; in the plain form the host round trips fall inside stage 1/2).
+// queued form; in the plain forms the host round trips fall inside stage 1/2).
 void run_gpu_stages_timed(BsfHandle* h, int n) {
-    if (h->mode == BSF_MODE_PLAIN) {
-        run_gpu_stages_plain(h, n);
+    if (h->mode == BSF_MODE_PLAIN || h->mode == BSF_MODE_PLAIN_SCREENED) {
+        if (h->mode == BSF_MODE_PLAIN) run_gpu_stages_plain(h, n);
+        else run_gpu_stages_plain_screened(h, n);
         record(h, 2);
         record(h, 3);
         return;
@@ -493,10 +566,20 @@ void enqueue_batch(BsfHandle* h, int n, int seedSource, const std::int64_t* seed
           "counts");
     check(cudaMemcpyAsync(h->hPinned + 14, h->dCoarseErr, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
           "coarse flag");
+    // the seeds the setup read: the caller's device array (seed source 0 with seeds given) or the handle's
+    const std::int64_t* seedSrc = (seedSource == 0 && seeds) ? seeds : h->dSeeds;
+    k_gather_exact<<<(h->exactCap + 127) / 128, 128, 0, h->stream>>>(h->dExactQueue, h->dCounters + 2, h->exactCap,
+                                                                     h->dRegions, seedSrc, h->centers,
+                                                                     h->dExactItems);
+    ++h->launches;
+    check(cudaGetLastError(), "k_gather_exact");
+    check(cudaMemcpyAsync(h->hExactItems, h->dExactItems, sizeof(ExactItem) * kExactPrefix, cudaMemcpyDeviceToHost,
+                          h->stream),
+          "exact items");
 }
 
-// Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters.
-constexpr int kBatchGraphKernels = 6;
+// Kernels in one batch graph: setup, Stage0, P19, coarse signs, coarse score, counters, exact gather.
+constexpr int kBatchGraphKernels = 7;
 
 // Batches of a Stage0 sweep between two host reads of the survivor list (the
 // list holds this many batches' worth, so it never overflows in between).
@@ -648,19 +731,19 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     read_stage_times(h);
     const auto exactStart = std::chrono::steady_clock::now();
     const int exactN = std::min(hcount[2], h->exactCap);
+    if (exactN > kExactPrefix)
+        d2h(h, h->hExactItems + kExactPrefix, h->dExactItems + kExactPrefix,
+            sizeof(ExactItem) * (exactN - kExactPrefix), "exact items");
+    // queue order varies between runs; records go out in (world, centre) order
+    std::vector<ExactItem> items(h->hExactItems, h->hExactItems + exactN);
+    std::sort(items.begin(), items.end(), [](const ExactItem& a, const ExactItem& b) {
+        return a.ref.world != b.ref.world ? a.ref.world < b.ref.world : a.ref.center < b.ref.center;
+    });
     std::vector<RegionRef> ex(exactN);
     std::vector<RegionInfo> info(exactN);
-    if (exactN) {
-        d2h(h, ex.data(), h->dExactQueue, sizeof(RegionRef) * exactN, "exact list");
-        std::sort(ex.begin(), ex.end(), [](const RegionRef& a, const RegionRef& b) {
-            return a.world != b.world ? a.world < b.world : a.center < b.center;
-        });
-        for (int k = 0; k < exactN; ++k)
-            check(cudaMemcpyAsync(&info[k],
-                                  h->dRegions + static_cast<std::size_t>(ex[k].world) * h->centers + ex[k].center,
-                                  sizeof(RegionInfo), cudaMemcpyDeviceToHost, h->stream),
-                  "region info");
-        check(cudaStreamSynchronize(h->stream), "region info");
+    for (int k = 0; k < exactN; ++k) {
+        ex[k] = items[k].ref;
+        info[k] = items[k].info;
     }
     // Exact stage: the regions are independent, so up to ectx.size() of them are
     // resolved at once, each by a host thread on its own stream and scratch.
@@ -700,10 +783,7 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
         if (isl.found) ++islands;
         if (written < recordsCap) {
             bsf_mega_record& r = records[written++];
-            std::int64_t seed = 0;
-            if (hostSeeds) seed = seeds[ex[k].world];
-            else d2h(h, &seed, seeds + ex[k].world, 8, "seed");
-            r.seed = seed;
+            r.seed = items[k].seed;
             r.world_index = ex[k].world;
             r.center_index = ex[k].center;
             r.center_chunk_x = ccx;
@@ -773,6 +853,7 @@ void open_buffers(BsfHandle* h, const bsf_config& cfg) {
     h->alloc(reinterpret_cast<void**>(&h->dHashes), n * 8, "hashes");
     h->alloc(reinterpret_cast<void**>(&h->dStageCounts), 8 * sizeof(unsigned long long), "stage counts");
     h->alloc(reinterpret_cast<void**>(&h->dExactQueue), h->exactCap * sizeof(RegionRef), "exact queue");
+    h->alloc(reinterpret_cast<void**>(&h->dExactItems), h->exactCap * sizeof(ExactItem), "exact items");
     h->fs.p19Capacity = static_cast<int>(regions);
     h->alloc(reinterpret_cast<void**>(&h->fs.p19Queue), regions * sizeof(RegionRef), "p19 queue");
     h->alloc(reinterpret_cast<void**>(&h->fs.highest), regions * 256, "p19 grids");
@@ -888,6 +969,8 @@ void* bsf_open(const bsf_config* cfgIn) {
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hOut), std::max<std::size_t>(h->outBytes, n * 4096)),
               "pinned output");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hSweep), 16 * sizeof(unsigned long long)), "pinned sweep");
+        check(cudaMallocHost(reinterpret_cast<void**>(&h->hExactItems), sizeof(ExactItem) * h->exactCap),
+              "pinned exact items");
         check(cudaMallocHost(reinterpret_cast<void**>(&h->hSweepOut), h->sweep.outCap * 8), "pinned sweep list");
         check(cudaStreamSynchronize(h->stream), "open");
         h->ok = true;
@@ -907,7 +990,7 @@ void bsf_close(void* hv) {
     void* dev[] = {h->dSeeds, h->cache.perms, h->cache.offsets, h->dRegions, h->dCoarseQueue, h->dCounters,
                    h->dSigns, h->dLabels, h->dStats, h->dOut, h->dHashes, h->dStageCounts, h->dExactQueue,
                    h->dExactBase, h->dIsland, h->dPrevMin, h->dPrevMax, h->fs.p19Queue, h->fs.highest,
-                   h->fs.p19Count, h->fs.stats, h->dSweepBase};
+                   h->fs.p19Count, h->fs.stats, h->dSweepBase, h->dExactItems};
     for (void* p : dev)
         if (p) cudaFree(p);
     for (auto& e : h->ev)
@@ -921,6 +1004,7 @@ void bsf_close(void* hv) {
     if (h->hOut) cudaFreeHost(h->hOut);
     if (h->hPinned) cudaFreeHost(h->hPinned);
     if (h->hSweep) cudaFreeHost(h->hSweep);
+    if (h->hExactItems) cudaFreeHost(h->hExactItems);
     if (h->hSweepOut) cudaFreeHost(h->hSweepOut);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -1008,7 +1092,8 @@ const char* bsf_last_error(const void* hv) {
 
 int bsf_set_mode(void* hv, int32_t mode) {
     return guarded(hv, [&](BsfHandle* h) {
-        if (mode != BSF_MODE_QUEUED && mode != BSF_MODE_PLAIN) throw std::invalid_argument("mode must be 0 or 1");
+        if (mode != BSF_MODE_QUEUED && mode != BSF_MODE_PLAIN && mode != BSF_MODE_PLAIN_SCREENED)
+            throw std::invalid_argument("mode must be 0, 1 or 2");
         h->mode = mode;
         return BSF_OK;
     });
@@ -1178,7 +1263,7 @@ int bsf_autotune(void* hv, uint32_t worlds, char* report, size_t reportLen) {
         auto stage0 = [&]() {
             check(cudaMemsetAsync(h->dCounters, 0, sizeof(int), h->stream), "memset");
             launch_stage0_fast(h->cache, n, h->centers, h->prof, h->dRegions, h->dCoarseQueue, h->dCounters,
-                               h->capacity * h->centers, h->fs, h->stream);
+                               h->capacity * h->centers, h->fs, h->stream, h->persistent);
         };
         int best = 0;
         float bestMs = 1e30f;
@@ -1199,7 +1284,7 @@ int bsf_autotune(void* hv, uint32_t worlds, char* report, size_t reportLen) {
             set_coarse_fast_variant(v);
             const float ms = time_it([&]() {
                 launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, nullptr,
-                                         h->stream);
+                                         h->stream, h->persistent);
             });
             std::snprintf(buf, sizeof(buf), " %s=%.2fms", coarse_fast_variant_name(v), ms);
             rep += buf;
@@ -1207,6 +1292,21 @@ int bsf_autotune(void* hv, uint32_t worlds, char* report, size_t reportLen) {
         }
         set_coarse_fast_variant(best);
         rep += std::string(" -> ") + coarse_fast_variant_name(best);
+        // grid shape with the chosen variants: persistent CTAs looping over worlds and
+        // half-regions, or one CTA per world pair and per half-region
+        float gridMs[2];
+        for (int persistent = 1; persistent >= 0; --persistent) {
+            h->persistent = persistent != 0;
+            gridMs[persistent] = time_it([&]() {
+                stage0();
+                launch_coarse_signs_fast(h->cache, h->dCoarseQueue, h->dCounters, h->coarseCap, h->dSigns, nullptr,
+                                         h->stream, h->persistent);
+            });
+        }
+        h->persistent = gridMs[1] <= gridMs[0];
+        std::snprintf(buf, sizeof(buf), "; grid: persistent=%.2fms per-item=%.2fms -> %s", gridMs[1], gridMs[0],
+                      h->persistent ? "persistent" : "per-item");
+        rep += buf;
         check(cudaStreamSynchronize(h->stream), "autotune");
         if (report && reportLen) {
             std::strncpy(report, rep.c_str(), reportLen - 1);

@@ -33,7 +33,8 @@ extern "C" {
 
 /* Pipeline forms for the batch entry points. */
 #define BSF_MODE_QUEUED 0 /* fused Stage0 kernel, device-side queues, one host sync per batch */
-#define BSF_MODE_PLAIN 1  /* one launch per stage, host round trip after every stage */
+#define BSF_MODE_PLAIN 1  /* one launch per stage, host round trip after every stage (FP64 kernels) */
+#define BSF_MODE_PLAIN_SCREENED 2 /* BSF_MODE_PLAIN's stage-by-stage driving of the queued form's kernels */
 
 typedef struct bsf_config {
     int32_t device;           /* CUDA device ordinal */
@@ -188,7 +189,9 @@ int bsf_last_stage_ms(const void* h, float* ms4);
 /* Autotuner: times every launch-shape variant (threads per CTA x CTAs per SM)
  * of the screened Stage0 and coarse kernels on `worlds` calibration worlds
  * (capacity permitting) with CUDA events and keeps the fastest for this
- * process. report (optional) receives "kernel: variant=ms ... -> choice". */
+ * process, then times the two grid shapes (bsf_set_persistent) with them and
+ * keeps the faster for this handle. report (optional) receives
+ * "kernel: variant=ms ... -> choice; grid: ... -> choice". */
 int bsf_autotune(void* h, uint32_t worlds, char* report, size_t report_len);
 /* Selects launch-shape variants explicitly (index order of the autotune report). */
 int bsf_set_launch_variants(void* h, int32_t stage0_variant, int32_t coarse_variant);

@@ -39,15 +39,26 @@ def test_screened_p20_equal_fp64():
 
 
 def test_mega_search_forms_agree():
+    """Queued (screened kernels, device queues, graphs), plain on the screened
+    kernels, and plain on the FP64 kernels: the same stage counts, region records
+    and islands."""
     seeds = consecutive(8192, 11)
     with bsf.Worker(capacity=8192, profile="mega", centers=8, max_exact_radius=24) as w:
         c1, r1 = w.mega_search(seeds)
+        g1 = w.last_region_records(8192)
+        w.set_mode(bsf.MODE_PLAIN_SCREENED)
+        c3, r3 = w.mega_search(seeds)
+        g3 = w.last_region_records(8192)
         w.set_mode(bsf.MODE_PLAIN)
         c2, r2 = w.mega_search(seeds)
-    d1, d2 = c1.as_dict(), c2.as_dict()
+    d1, d2, d3 = c1.as_dict(), c2.as_dict(), c3.as_dict()
     for k in ("rng_fallbacks", "screened_tasks", "fallback_tasks"):  # instrumentation, not results
-        d1.pop(k), d2.pop(k)
-    assert d1 == d2
+        d1.pop(k), d2.pop(k), d3.pop(k)
+    assert d1 == d2 == d3
+    assert np.array_equal(g1, g3)
+    assert c3.screened_tasks == c1.screened_tasks  # the same screened kernels ran
+    assert [(r.world_index, r.center_index, r.coarse, r.island.key()) for r in r3] == \
+           [(r.world_index, r.center_index, r.coarse, r.island.key()) for r in r1]
     # the screening must decide the vast majority of columns without FP64
     assert c1.screened_tasks > 0 and c1.fallback_tasks < 0.01 * c1.screened_tasks
     assert [(r.world_index, r.center_index, r.coarse, r.island.key()) for r in r1] == \
@@ -140,3 +151,23 @@ def test_exact_fallback_paths_alone_match_fp64():
     assert cf.fallback_tasks == cf.screened_tasks > 0
     assert [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rf] == \
            [(x.world_index, x.center_index, x.coarse, x.island.key()) for x in rp]
+
+
+def test_device_seed_records_carry_their_seeds_in_every_form():
+    """bsf_mega_search_device in the three forms: each record's seed is the seed at
+    its world index (gathered on the device with the region's outcome), and the
+    records equal those of bsf_mega_search on the same seeds from host memory."""
+    torch = pytest.importorskip("torch")
+    seeds = consecutive(8192, 12)
+    d = torch.from_numpy(seeds).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    with bsf.Worker(capacity=8192, profile="mega", centers=8, max_exact_radius=24) as w:
+        _, host = w.mega_search(seeds)
+        want = [(r.seed, r.world_index, r.center_index, r.coarse, r.island.key()) for r in host]
+        assert want, "the batch reaches the exact stage"
+        for mode in (bsf.MODE_QUEUED, bsf.MODE_PLAIN_SCREENED, bsf.MODE_PLAIN):
+            w.set_mode(mode)
+            _, recs = w.mega_search_device(d.data_ptr(), len(seeds), stream=stream)
+            got = [(r.seed, r.world_index, r.center_index, r.coarse, r.island.key()) for r in recs]
+            assert got == want, mode
+            assert all(r.seed == seeds[r.world_index] for r in recs)
