@@ -5,7 +5,9 @@
  * name ends in _device (device pointers + a cudaStream_t passed as void*).
  * Every function returns BSF_OK (0) or a negative BSF_E_* status; the message
  * of the last failure on a handle is available from bsf_last_error(). No C++
- * exception crosses this boundary. A handle serves one request at a time
+ * exception crosses this boundary. A request of count == 0 is BSF_E_ARG here;
+ * the worker's stream modes read a zero count as the end of the stream, as the
+ * reference worker does. A handle serves one request at a time
  * (the reference worker is single-request too: GpuStage0Scout.filter is
  * synchronized, src/GpuStage0Scout.java:249); use one handle per thread.
  */
