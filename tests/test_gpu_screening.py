@@ -67,15 +67,19 @@ def test_mega_search_forms_agree():
 
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_every_launch_variant_gives_identical_records(variant):
-    seeds = consecutive(2048, 300 + variant)
-    with bsf.Worker(capacity=2048, profile="general", research=True, centers=8, max_exact_radius=1) as w:
+    """Every Stage0 and coarse launch shape, on both grid shapes, against the FP64
+    form."""
+    seeds = consecutive(2049, 300 + variant)  # odd: the last pass holds one world
+    with bsf.Worker(capacity=2049, profile="general", research=True, centers=8, max_exact_radius=1) as w:
         w.set_mode(bsf.MODE_PLAIN)
         exact = w.stage0_filter(seeds)
         w.set_mode(bsf.MODE_QUEUED)
         w.set_launch_variants(variant, variant)
-        fast = w.stage0_filter(seeds)
+        for persistent in (True, False):
+            w.set_persistent(persistent)
+            fast = w.stage0_filter(seeds)
+            assert np.array_equal(fast, exact), (variant, persistent)
         w.set_launch_variants(0, 0)
-    assert np.array_equal(fast, exact)
 
 
 def test_autotune_reports_and_keeps_results_exact():
