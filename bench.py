@@ -8,9 +8,13 @@ terrain scan (+ border verify + hot scan) for coarse survivors. Seeds are
 seeded synthetic consecutive 48-bit values (the full-pipeline workload over
 2^36 consecutive seeds, sampled one batch per step).
 
-  value  : worlds/s with seeds already resident in HBM (bsf_mega_search_device),
-           CUDA events on the stream the kernels run on.
-  e2e    : worlds/s through bsf_mega_search with host seeds (H2D + D2H inside).
+  value  : worlds/s with seeds already resident in HBM: the timed batches as one
+           pipelined range (bsf_mega_search_range_device, each batch's exact
+           stage overlapping the next batch's GPU stages), CUDA events on the
+           caller's stream around the call. The same batches one call each
+           (bsf_mega_search_device) give the per-stage times.
+  e2e    : the same seeds from host memory through bsf_mega_search_range (H2D of
+           seeds and D2H of counts and records inside).
   forms  : the plain stage-by-stage form and the served form (bsf.Server: range
            requests in chunks over several lanes, previews arriving meanwhile)
            on the same kind of workload, with preview latency alone and mixed.
@@ -646,8 +650,12 @@ def main():
     tune_report = "off (default launch shapes)" if args.no_autotune else worker.autotune(min(B, 4096))
     for s in range(W):
         worker.mega_search_device(d_seeds[s].data_ptr(), B, radius=args.radius, stream=sptr)
+    # the pipelined range opens its second handle and captures its graphs here
+    worker.mega_search_range_device(d_seeds[0].data_ptr(), W * B, radius=args.radius, stream=sptr)
     torch.cuda.synchronize()
 
+    # value: the K timed batches as one pipelined range (bsf_mega_search_range_device):
+    # each batch's exact stage overlaps the next batch's GPU stages
     clocks = ClockSampler(dist.local)
     clocks.start()
     time.sleep(0.4)
@@ -656,18 +664,8 @@ def main():
     l0 = worker.kernel_launches
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    totals = None
-    stage = [0.0, 0.0, 0.0, 0.0]
-    records = 0
-    dev_recs = []
-    for s in range(K):
-        counts, recs = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
-        d = counts.as_dict()
-        totals = d if totals is None else {k: totals[k] + d[k] for k in d}
-        st = worker.last_stage_ms()
-        stage = [a + b for a, b in zip(stage, st)]
-        records += len(recs)
-        dev_recs.append(recs)
+    rcounts, range_recs = worker.mega_search_range_device(d_seeds[W].data_ptr(), K * B, radius=args.radius,
+                                                          stream=sptr)
     e1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()
@@ -676,29 +674,44 @@ def main():
     clk = clocks.stop()
     ms_max = dist.max(ms)
     value = B * K * dist.world / (ms_max / 1e3)
+    totals = rcounts.as_dict()
+    records = len(range_recs)
 
-    # e2e: the same seeds as the device-timed steps, from host memory through the
-    # public API (H2D seeds, D2H counts + records inside the timed region).
-    host_blocks = [d_seeds[W + s].cpu().numpy() for s in range(K)]
-    worker.mega_search(d_seeds[0].cpu().numpy(), radius=args.radius)
-    dist.barrier()
+    # the same batches one call per batch (bsf_mega_search_device, no overlap between
+    # batches): the per-stage event times of each batch
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_records = 0
-    e2e_recs = []
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b0.record(stream)
+    stage = [0.0, 0.0, 0.0, 0.0]
+    batch_recs = []
     for s in range(K):
-        _, recs = worker.mega_search(host_blocks[s], radius=args.radius)
-        e2e_records += len(recs)
-        e2e_recs.append(recs)
+        counts, recs = worker.mega_search_device(d_seeds[W + s].data_ptr(), B, radius=args.radius, stream=sptr)
+        stage = [a + b for a, b in zip(stage, worker.last_stage_ms())]
+        batch_recs += [(r.seed, r.world_index + s * B, r.center_index, r.coarse, r.island.key()) for r in recs]
+    b1.record(stream)
     torch.cuda.synchronize()
-    e2e_s = dist.max(time.perf_counter() - t0)
+    batch_calls = B * K / (b0.elapsed_time(b1) / 1e3)
 
     def rec_keys(rs):
         return [(r.seed, r.world_index, r.center_index, r.coarse, r.island.key()) for r in rs]
-    e2e_same = all(rec_keys(a) == rec_keys(b) for a, b in zip(dev_recs, e2e_recs))
+    range_same_as_batches = rec_keys(range_recs) == batch_recs
+
+    # e2e: the same seeds from host memory through the public API's pipelined range
+    # (bsf_mega_search_range: H2D of each batch's seeds and D2H of counts and records
+    # inside the timed region)
+    host_seeds = d_seeds[W:W + K].reshape(-1).cpu().numpy()
+    worker.mega_search_range(d_seeds[0:W].reshape(-1).cpu().numpy(), radius=args.radius)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, e2e_recs = worker.mega_search_range(host_seeds, radius=args.radius)
+    torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = B * K * dist.world / e2e_s
+    e2e_records = len(e2e_recs)
+    e2e_same = rec_keys(e2e_recs) == rec_keys(range_recs)
     rec_bytes = __import__("ctypes").sizeof(bsf.MegaRecord)
-    d2h = 8 * 8 + 4 * 4 + (e2e_records / max(1, K)) * (rec_bytes + 48)
+    d2h = 8 * 8 + 4 * 4 + (e2e_records / max(1, K)) * (rec_bytes + 64)
 
     extras = {}
     if dist.rank == 0 and not args.skip_extras:
@@ -788,8 +801,9 @@ def main():
             worker.preview(int(splitmix(args.seed, 1000 + i) & ((1 << 48) - 1)), 0, 0, args.radius)
             lat.append((time.perf_counter() - t) * 1e3)
         lat.sort()
-        extras["preview_ms"] = {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                                "n": len(lat), "radius": args.radius}
+        if lat:
+            extras["preview_ms"] = {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                                    "n": len(lat), "radius": args.radius}
 
     if dist.rank == 0:
         stage0_ms = stage[1] / K
@@ -812,7 +826,10 @@ def main():
                        "autotune": tune_report},
             "e2e": {"value": e2e_value, "unit": "worlds/s", "h2d_bytes_per_step": B * 8,
                     "d2h_bytes_per_step": int(d2h), "seeds": "the device-timed steps' seeds, from host memory",
-                    "records_equal_to_value_run": e2e_same},
+                    "api": "bsf_mega_search_range", "records_equal_to_value_run": e2e_same},
+            "pipeline": {"value_api": "bsf_mega_search_range_device over the %d timed batches" % K,
+                         "batch_calls_worlds_per_s": batch_calls, "range_over_batch_calls": value / dist.world /
+                         batch_calls, "records_equal_to_batch_calls": range_same_as_batches},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "kernel": "k_stage0_fast", "achieved": achieved / 1e12,
                          "peak": fp32_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp32_peak,

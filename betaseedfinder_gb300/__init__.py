@@ -118,6 +118,7 @@ PENDING = 1
 EXPORTS = ["bsf_default_config", "bsf_default_match_settings", "bsf_open", "bsf_close", "bsf_last_error",
            "bsf_set_mode", "bsf_stage0_filter", "bsf_stage0_sweep", "bsf_p20_filter", "bsf_chunk_bitmaps", "bsf_exact_scan",
            "bsf_resolve_region", "bsf_preview", "bsf_mega_search", "bsf_mega_search_device",
+           "bsf_mega_search_range", "bsf_mega_search_range_device",
            "bsf_kernel_launches", "bsf_device_summary", "bsf_screen_probe", "bsf_last_stage_ms", "bsf_measure_peaks", "bsf_chunk_bitmaps_noalloc",
            "bsf_autotune", "bsf_set_launch_variants", "bsf_config_footprint", "bsf_handle_footprint",
            "bsf_set_stream_priority", "bsf_set_persistent", "bsf_set_screening", "bsf_set_profile", "bsf_last_region_records", "bsf_default_server_config", "bsf_server_open", "bsf_server_close",
@@ -160,6 +161,11 @@ def load(path=LIB_PATH):
     L.bsf_mega_search_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int32, P(MatchSettings),
                                          P(MegaRecord), ctypes.c_uint32, P(ctypes.c_uint32), P(StageCounts),
                                          ctypes.c_void_p]
+    L.bsf_mega_search_range.argtypes = [vp, i64p, ctypes.c_uint64, ctypes.c_int32, P(MatchSettings), P(MegaRecord),
+                                        ctypes.c_uint32, P(ctypes.c_uint32), P(StageCounts)]
+    L.bsf_mega_search_range_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
+                                               P(MatchSettings), P(MegaRecord), ctypes.c_uint32, P(ctypes.c_uint32),
+                                               P(StageCounts), ctypes.c_void_p]
     L.bsf_kernel_launches.argtypes = [vp]
     L.bsf_kernel_launches.restype = ctypes.c_uint64
     L.bsf_last_stage_ms.argtypes = [vp, P(ctypes.c_float)]
@@ -422,6 +428,29 @@ class Worker:
         self._check(load().bsf_mega_search_device(self._h, ctypes.c_void_p(d_seeds_ptr), count, radius,
                                                   ctypes.byref(s), recs, records_cap, ctypes.byref(n),
                                                   ctypes.byref(counts), ctypes.c_void_p(stream or 0)))
+        return counts, [recs[i] for i in range(n.value)]
+
+
+    def mega_search_range(self, seeds, radius=7, settings=None, records_cap=1 << 16):
+        """Pipelined MEGA search over a seed array of any length (bsf_mega_search_range)."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        s = settings or default_match_settings()
+        recs = (MegaRecord * records_cap)()
+        n = ctypes.c_uint32(0)
+        counts = StageCounts()
+        self._check(load().bsf_mega_search_range(self._h, _p(seeds, ctypes.c_int64), len(seeds), radius,
+                                                 ctypes.byref(s), recs, records_cap, ctypes.byref(n),
+                                                 ctypes.byref(counts)))
+        return counts, [recs[i] for i in range(n.value)]
+
+    def mega_search_range_device(self, d_seeds_ptr, count, radius=7, settings=None, records_cap=1 << 16, stream=None):
+        s = settings or default_match_settings()
+        recs = (MegaRecord * records_cap)()
+        n = ctypes.c_uint32(0)
+        counts = StageCounts()
+        self._check(load().bsf_mega_search_range_device(self._h, ctypes.c_void_p(d_seeds_ptr), count, radius,
+                                                        ctypes.byref(s), recs, records_cap, ctypes.byref(n),
+                                                        ctypes.byref(counts), ctypes.c_void_p(stream or 0)))
         return counts, [recs[i] for i in range(n.value)]
 
 

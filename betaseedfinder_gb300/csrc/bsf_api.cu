@@ -230,6 +230,9 @@ struct BsfHandle {
         int variants;  // launch-shape variants the graph was captured with
     };
     std::vector<std::pair<long long, CachedGraph>> graphs;  // batch graphs by (worlds, seed source)
+    BsfHandle* twin = nullptr;           // second handle of the pipelined range search (mega_range)
+    bool exactHigh = false;              // exact-scan contexts 1.. on the highest-priority streams
+    cudaEvent_t rangeEvent = nullptr;    // orders a range search after the caller's stream
 
     void drop_graphs() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second.exec);
@@ -699,17 +702,8 @@ void stage0_sweep(BsfHandle* h, std::int64_t start, std::uint64_t count, std::in
     }
 }
 
-int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, uint32_t count,
-               int32_t radius, const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
-               uint32_t* recordsCount, bsf_stage_counts* counts) {
-    if (!seeds || count == 0 || count > static_cast<uint32_t>(h->capacity) || (!records && recordsCap))
-        throw std::invalid_argument("bsf_mega_search: bad seeds/count/records");
-    if (radius < 0 || radius > h->exact.maxRadius) throw std::length_error("radius exceeds max_exact_radius");
-    const MatchSettings ms = to_ms(s);
-    cudaStream_t saved = h->stream;
-    if (userStream) h->stream = userStream;
-    const int n = static_cast<int>(count);
-    const int regions = n * h->centers;
+// Enqueues the GPU part of a batch of n worlds on h->stream, without a host sync.
+void mega_begin(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, int n) {
     if (h->mode == BSF_MODE_QUEUED) {
         // Queued form: one CUDA graph per (batch size, seed source) replays the
         // whole GPU part of the batch; the seeds reach the handle's buffers first.
@@ -721,6 +715,35 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
     } else {
         enqueue_batch(h, n, hostSeeds ? 1 : 0, seeds);
     }
+}
+
+void mega_end(BsfHandle* h, uint32_t count, int32_t radius, const MatchSettings& ms, bsf_mega_record* records,
+              uint32_t recordsCap, uint32_t* recordsCount, bsf_stage_counts* counts);
+
+int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, uint32_t count,
+               int32_t radius, const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
+               uint32_t* recordsCount, bsf_stage_counts* counts) {
+    if (!seeds || count == 0 || count > static_cast<uint32_t>(h->capacity) || (!records && recordsCap))
+        throw std::invalid_argument("bsf_mega_search: bad seeds/count/records");
+    if (radius < 0 || radius > h->exact.maxRadius) throw std::length_error("radius exceeds max_exact_radius");
+    const MatchSettings ms = to_ms(s);
+    struct StreamRestore {
+        BsfHandle* h;
+        cudaStream_t saved;
+        ~StreamRestore() { h->stream = saved; }
+    } restore{h, h->stream};
+    if (userStream) h->stream = userStream;
+    mega_begin(h, seeds, hostSeeds, static_cast<int>(count));
+    mega_end(h, count, radius, ms, records, recordsCap, recordsCount, counts);
+    return BSF_OK;
+}
+
+// Waits for the GPU part of the batch mega_begin enqueued, runs its exact stage
+// and writes its records (world_index within the batch) and stage counts.
+void mega_end(BsfHandle* h, uint32_t count, int32_t radius, const MatchSettings& ms, bsf_mega_record* records,
+              uint32_t recordsCap, uint32_t* recordsCount, bsf_stage_counts* counts) {
+    const int n = static_cast<int>(count);
+    const int regions = n * h->centers;
     unsigned long long* hc = h->hPinned;
     unsigned long long* hs = h->hPinned + 8;
     const int* hcount = reinterpret_cast<const int*>(h->hPinned + 12);
@@ -821,8 +844,103 @@ int mega_batch(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStre
         counts->screened_tasks = h->mode == BSF_MODE_PLAIN ? 0 : hs[0] + hs[2];
         counts->fallback_tasks = h->mode == BSF_MODE_PLAIN ? 0 : hs[1] + hs[3];
     }
-    h->stream = saved;
-    return BSF_OK;
+}
+
+// The pipeline's second handle: same config and settings, its own buffers,
+// streams, graphs and exact-scan contexts. Opened on first use.
+BsfHandle* twin_of(BsfHandle* h) {
+    if (!h->twin) {
+        void* t = bsf_open(&h->cfg);
+        if (!t) throw std::runtime_error("out of memory opening the pipeline's second handle");
+        BsfHandle* tw = static_cast<BsfHandle*>(t);
+        if (!tw->ok) {
+            const std::string msg = "opening the pipeline's second handle: " + tw->err;
+            bsf_close(t);
+            throw std::runtime_error(msg);
+        }
+        h->twin = tw;
+    }
+    BsfHandle* t = h->twin;
+    t->mode = h->mode;
+    t->persistent = h->persistent;
+    t->prof = h->prof;
+    t->cfg.profile = h->cfg.profile;
+    t->fs.forceExact = h->fs.forceExact;
+    return t;
+}
+
+// Exact-scan streams of the batch exact stage (contexts 1..) at the device's
+// highest priority (or the default): in a pipelined range the next batch's
+// Stage0 CTAs hold nearly all of each SM's shared memory, so an exact-scan
+// kernel only starts when one of them retires, and at equal priority the block
+// scheduler would start the next queued Stage0 CTA instead.
+void set_exact_priority(BsfHandle* h, bool high) {
+    if (h->exactHigh == high) return;
+    int least = 0, greatest = 0;
+    check(cudaDeviceGetStreamPriorityRange(&least, &greatest), "priority range");
+    for (std::size_t t = 1; t < h->ectx.size(); ++t) {
+        ExactCtx& x = h->ectx[t];
+        cudaStream_t s = nullptr;
+        check(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, high ? greatest : least), "stream");
+        if (x.stream) {
+            check(cudaStreamSynchronize(x.stream), "stream");
+            cudaStreamDestroy(x.stream);
+        }
+        x.stream = s;
+    }
+    h->exactHigh = high;
+}
+
+// Pipelined MEGA search over `count` worlds: batches of the handle's capacity
+// alternate between h and its twin, and each batch's GPU part is enqueued
+// before the previous batch's exact stage runs, so that exact stage (host
+// threads, exact-context streams) overlaps the next batch's GPU stages.
+void mega_range(BsfHandle* h, const std::int64_t* seeds, bool hostSeeds, cudaStream_t userStream, std::uint64_t count,
+                int32_t radius, const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
+                uint32_t* recordsCount, bsf_stage_counts* counts) {
+    if (!seeds || count == 0 || count >= (1ull << 31) || (!records && recordsCap))
+        throw std::invalid_argument("bsf_mega_search_range: bad seeds/count/records (count must be 1..2^31-1)");
+    if (radius < 0 || radius > h->exact.maxRadius) throw std::length_error("radius exceeds max_exact_radius");
+    const MatchSettings ms = to_ms(s);
+    BsfHandle* hs[2] = {h, twin_of(h)};
+    for (BsfHandle* x : hs) set_exact_priority(x, true);
+    if (userStream) {
+        // work the caller queued before the call (e.g. writing the seeds) comes first
+        if (!h->rangeEvent) check(cudaEventCreateWithFlags(&h->rangeEvent, cudaEventDisableTiming), "event");
+        check(cudaEventRecord(h->rangeEvent, userStream), "event");
+        for (BsfHandle* x : hs) check(cudaStreamWaitEvent(x->stream, h->rangeEvent, 0), "stream wait");
+    }
+    const std::uint64_t cap = static_cast<std::uint64_t>(h->capacity);
+    auto batchAt = [&](std::uint64_t off) { return static_cast<int>(std::min<std::uint64_t>(cap, count - off)); };
+    bsf_stage_counts total{};
+    uint32_t written = 0;
+    std::uint64_t off = 0;
+    int k = 0;
+    try {
+        mega_begin(hs[0], seeds, hostSeeds, batchAt(0));
+        while (off < count) {
+            BsfHandle* cur = hs[k & 1];
+            const int n = batchAt(off);
+            const std::uint64_t next = off + static_cast<std::uint64_t>(n);
+            if (next < count) mega_begin(hs[(k + 1) & 1], seeds + next, hostSeeds, batchAt(next));
+            uint32_t w = 0;
+            bsf_stage_counts c{};
+            mega_end(cur, static_cast<uint32_t>(n), radius, ms, records ? records + written : nullptr,
+                     recordsCap - written, &w, &c);
+            for (uint32_t i = 0; i < w; ++i) records[written + i].world_index += static_cast<int32_t>(off);
+            written += w;
+            std::uint64_t* dst = &total.worlds;
+            const std::uint64_t* src = &c.worlds;
+            for (std::size_t f = 0; f < sizeof(bsf_stage_counts) / sizeof(std::uint64_t); ++f) dst[f] += src[f];
+            off = next;
+            ++k;
+        }
+    } catch (...) {
+        for (BsfHandle* x : hs) cudaStreamSynchronize(x->stream);  // no batch left in flight
+        throw;
+    }
+    if (recordsCount) *recordsCount = written;
+    if (counts) *counts = total;
 }
 
 // Every device buffer of a handle, sized from its config. With h->dry set this
@@ -984,6 +1102,8 @@ void* bsf_open(const bsf_config* cfgIn) {
 void bsf_close(void* hv) {
     BsfHandle* h = static_cast<BsfHandle*>(hv);
     if (!h) return;
+    if (h->twin) bsf_close(h->twin);
+    if (h->rangeEvent) cudaEventDestroy(h->rangeEvent);
     if (h->stream) cudaStreamSynchronize(h->stream);
     std::unique_lock<std::shared_mutex> allocLock(capture_guard());
     h->drop_graphs();
@@ -1026,7 +1146,7 @@ int bsf_config_footprint(const bsf_config* cfg, uint64_t* bytes) {
 
 uint64_t bsf_handle_footprint(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
-    return h ? h->footprint : 0;
+    return h ? h->footprint + (h->twin ? h->twin->footprint : 0) : 0;
 }
 
 int bsf_last_region_records(void* hv, uint8_t* out, size_t outLen) {
@@ -1234,6 +1354,25 @@ int bsf_stage0_sweep(void* hv, int64_t startSeed, uint64_t count, int64_t* survi
     });
 }
 
+int bsf_mega_search_range(void* hv, const int64_t* seeds, uint64_t count, int32_t radius, const bsf_match_settings* s,
+                          bsf_mega_record* records, uint32_t recordsCap, uint32_t* recordsCount,
+                          bsf_stage_counts* counts) {
+    return guarded(hv, [&](BsfHandle* h) {
+        mega_range(h, seeds, true, nullptr, count, radius, s, records, recordsCap, recordsCount, counts);
+        return BSF_OK;
+    });
+}
+
+int bsf_mega_search_range_device(void* hv, const int64_t* dSeeds, uint64_t count, int32_t radius,
+                                 const bsf_match_settings* s, bsf_mega_record* records, uint32_t recordsCap,
+                                 uint32_t* recordsCount, bsf_stage_counts* counts, void* stream) {
+    return guarded(hv, [&](BsfHandle* h) {
+        mega_range(h, dSeeds, false, static_cast<cudaStream_t>(stream), count, radius, s, records, recordsCap,
+                   recordsCount, counts);
+        return BSF_OK;
+    });
+}
+
 int bsf_last_stage_ms(const void* hv, float* ms4) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
     if (!h || !ms4) return BSF_E_ARG;
@@ -1374,7 +1513,8 @@ int bsf_device_summary(int32_t device, char* out, size_t outLen) {
 
 uint64_t bsf_kernel_launches(const void* hv) {
     const BsfHandle* h = static_cast<const BsfHandle*>(hv);
-    return h ? h->launches.load() : 0;
+    if (!h) return 0;
+    return h->launches.load() + (h->twin ? h->twin->launches.load() : 0);
 }
 
 }  // extern "C"

@@ -169,6 +169,27 @@ int bsf_mega_search_device(void* h, const int64_t* d_seeds, uint32_t count, int3
                            const bsf_match_settings* s, bsf_mega_record* records, uint32_t records_cap,
                            uint32_t* records_count, bsf_stage_counts* counts, void* stream);
 
+/* Pipelined MEGA search over `count` worlds (1 .. 2^31-1, any multiple of the
+ * capacity): batches of capacity worlds alternate between this handle and a
+ * second one it opens on first use with the same config (so twice the device
+ * memory; bsf_handle_footprint counts both), and each batch's GPU stages are
+ * enqueued before the previous batch's exact stage runs, so the exact stage
+ * (host threads and exact-scan streams) overlaps the next batch's GPU work.
+ * Records come in (world_index, center_index) order with world_index counted
+ * from the start of the range; counts are summed over the batches. The reference
+ * overlaps the same two parts across processes: the worker streams Stage0 and
+ * coarse records while the Java app's exact-scan threads drain its survivor
+ * queue (src/IslandSearchEngine.java:1225, 1437-1443). bsf_last_region_records
+ * and bsf_last_stage_ms describe this handle's own last batch only. */
+int bsf_mega_search_range(void* h, const int64_t* seeds, uint64_t count, int32_t radius, const bsf_match_settings* s,
+                          bsf_mega_record* records, uint32_t records_cap, uint32_t* records_count,
+                          bsf_stage_counts* counts);
+/* bsf_mega_search_range on device-resident seeds; the pipeline's streams wait for
+ * the work queued on `stream` (a cudaStream_t, NULL = none) before they start. */
+int bsf_mega_search_range_device(void* h, const int64_t* d_seeds, uint64_t count, int32_t radius,
+                                 const bsf_match_settings* s, bsf_mega_record* records, uint32_t records_cap,
+                                 uint32_t* records_count, bsf_stage_counts* counts, void* stream);
+
 /* Stage outcomes of every region of the last bsf_mega_search(_device) batch:
  * count * centers 34-byte research records (the stage0stream research layout,
  * world-major, centre-minor), e.g. to sample rejected regions for exact audits. */
@@ -179,7 +200,8 @@ int bsf_last_region_records(void* h, uint8_t* out, size_t out_len);
  * "Compute units: N", "Global memory: G GiB", one per line, into out. */
 int bsf_device_summary(int32_t device, char* out, size_t out_len);
 
-/* Number of GPU kernel launches issued by the handle so far (instrumentation). */
+/* Number of GPU kernel launches issued by the handle (and the second handle of
+ * its pipelined range search) so far (instrumentation). */
 uint64_t bsf_kernel_launches(const void* h);
 
 /* Device time of each stage of the last batch call, from CUDA events recorded

@@ -175,3 +175,32 @@ def test_device_seed_records_carry_their_seeds_in_every_form():
             got = [(r.seed, r.world_index, r.center_index, r.coarse, r.island.key()) for r in recs]
             assert got == want, mode
             assert all(r.seed == seeds[r.world_index] for r in recs)
+
+
+def test_pipelined_range_equals_batch_calls():
+    """bsf_mega_search_range(_device): 3.25 batches pipelined over the handle and its
+    twin give the records (world index counted from the range start) and summed
+    stage counts of one bsf_mega_search call per batch."""
+    torch = pytest.importorskip("torch")
+    cap = 4096
+    seeds = consecutive(cap * 3 + cap // 4, 21)
+    with bsf.Worker(capacity=cap, profile="mega", centers=8, max_exact_radius=24) as w:
+        want, wc = [], None
+        for off in range(0, len(seeds), cap):
+            c, r = w.mega_search(seeds[off:off + cap])
+            want += [(x.seed, x.world_index + off, x.center_index, x.coarse, x.island.key()) for x in r]
+            d = c.as_dict()
+            wc = d if wc is None else {k: wc[k] + d[k] for k in d}
+        single = w.footprint
+        c1, r1 = w.mega_search_range(seeds)
+        assert w.footprint == 2 * single  # the twin holds the same buffers
+        d = torch.from_numpy(seeds).cuda()
+        c2, r2 = w.mega_search_range_device(d.data_ptr(), len(seeds), stream=torch.cuda.current_stream().cuda_stream)
+    assert want, "the range reaches the exact stage"
+    for c, r in ((c1, r1), (c2, r2)):
+        assert [(x.seed, x.world_index, x.center_index, x.coarse, x.island.key()) for x in r] == want
+        got = c.as_dict()
+        for k in ("rng_fallbacks", "screened_tasks", "fallback_tasks"):
+            got.pop(k), wc.pop(k, None)
+        assert got == {k: v for k, v in wc.items() if k in got}
+    assert all(x.seed == seeds[x.world_index] for x in r1)
