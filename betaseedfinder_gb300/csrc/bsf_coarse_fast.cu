@@ -17,6 +17,7 @@
 #include "bsf_internal.h"
 #include "bsf_screen.cuh"
 
+#include <cmath>
 #include <cstdio>
 #include <stdexcept>
 
@@ -31,6 +32,8 @@ constexpr int HALF_ROWS = 31;  // X rows of the first half; the second has 30
 constexpr int NOCT = 66;
 constexpr int HALF_COLS = HALF_ROWS * SIDE;  // columns of the larger half-region
 
+__constant__ float2 cc_octave_scale[NOCT];  // octave_scale(o) split into a float pair
+
 struct CoarseSmem {
     std::uint8_t perm[ST_COUNT * PERM_BYTES];
     double off[ST_COUNT][3];
@@ -42,6 +45,7 @@ struct CoarseSmem {
     std::uint32_t mask[HALF_COLS];
     std::uint16_t climate[HALF_COLS];  // columns whose d5 needs the climate and noise4
     float4 clim[10];                   // climate generators' offsets as float pairs (climate_split)
+    float2 offSplit[NOCT][2];          // the lattice octaves' X (a) and Z (c) offsets as float pairs
     int cursor, screened, fallbacks, climateCount;
 };
 
@@ -152,7 +156,14 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             uint4* dst = reinterpret_cast<uint4*>(s.perm);
             for (int k = tid; k < WORLD_PERM_BYTES / 16; k += CT) dst[k] = src[k];
             const double* o = cache.offsets + static_cast<std::size_t>(ref.world) * WORLD_OFFSETS;
-            for (int k = tid; k < ST_COUNT * 3; k += CT) s.off[k / 3][k % 3] = o[(k / 3) * 4 + (k % 3)];
+            for (int k = tid; k < ST_COUNT * 3; k += CT) {
+                const double v = o[(k / 3) * 4 + (k % 3)];
+                s.off[k / 3][k % 3] = v;
+                if (k / 3 < NOCT && k % 3 != 1) {
+                    const DF d = df_of(v);
+                    s.offSplit[k / 3][(k % 3) / 2] = make_float2(d.h, d.l);
+                }
+            }
         }
         __syncthreads();
         if (tid < OCT3) {
@@ -168,14 +179,24 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
         }
         for (int e = tid; e < NOCT * (rows + SIDE); e += CT) {
             const int o = e / (rows + SIDE), k = e % (rows + SIDE);
+            // double-float entries (bsf_screen.cuh make_axis_df), FP64 where a floor is too close to call
+            const float2 sc = cc_octave_scale[o];
             if (k < rows) {
-                const AxisF ax = make_axis(static_cast<double>(originX + row0 + k) * octave_scale(o), s.off[o][0]);
+                const int coord = originX + row0 + k;
+                const float2 of = s.offSplit[o][0];
+                AxisF ax;
+                if (!make_axis_df(coord, DF{sc.x, sc.y}, DF{of.x, of.y}, ax))
+                    ax = make_axis(static_cast<double>(coord) * octave_scale(o), s.off[o][0]);
                 s.xf[o][k] = ax.f;
                 s.xd[o][k] = ax.fd;
                 s.xi[o][k] = static_cast<std::uint8_t>(ax.i);
             } else {
                 const int kz = k - rows;
-                const AxisF az = make_axis(static_cast<double>(originZ + kz) * octave_scale(o), s.off[o][2]);
+                const int coord = originZ + kz;
+                const float2 of = s.offSplit[o][1];
+                AxisF az;
+                if (!make_axis_df(coord, DF{sc.x, sc.y}, DF{of.x, of.y}, az))
+                    az = make_axis(static_cast<double>(coord) * octave_scale(o), s.off[o][2]);
                 s.zf[o][kz] = az.f;
                 s.zd[o][kz] = az.fd;
                 s.zi[o][kz] = static_cast<std::uint8_t>(az.i);
@@ -301,6 +322,15 @@ void set_coarse_fast_variant(int v) { g_variant = (v >= 0 && v < kVariants) ? v 
 int get_coarse_fast_variant() { return g_variant; }
 
 void init_coarse_fast() {
+    float2 scales[NOCT];
+    for (int o = 0; o < NOCT; ++o) {  // octave_scale(o) in the same IEEE operations as the device
+        const double base = o < 32 ? NOISE_XZ : (o < 40 ? NOISE_XZ / 80.0 : (o < 50 ? 1.121 : 200.0));
+        const int k = o < 16 ? o : (o < 32 ? o - 16 : (o < 40 ? o - 32 : (o < 50 ? o - 40 : o - 50)));
+        const double v = base * std::ldexp(1.0, -k);
+        const float h = static_cast<float>(v);
+        scales[o] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+    }
+    check(cudaMemcpyToSymbol(cc_octave_scale, scales, sizeof(scales)), "octave scales");
     int dev = 0, sms = 0;
     check(cudaGetDevice(&dev), "device");
     check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
