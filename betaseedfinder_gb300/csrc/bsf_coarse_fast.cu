@@ -121,14 +121,17 @@ __device__ __noinline__ void coarse_shape_climate(const CoarseSmem& s, int cx, i
     sh[1] = d5.e;
 }
 
-template <int Y0, int N>
-__device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz, const float* shape, unsigned& bits) {
+// Screened signs of levels [y0, y0 + n), n <= 6, from the column's shape; one
+// instantiation for all three level ranges (three had thrashed the instruction
+// cache whenever warps worked on different ranges).
+__device__ __noinline__ bool screened_range(const CoarseSmem& s, int kx, int kz, const float* shape, int y0, int n,
+                                            unsigned& bits) {
     if (shape[1] < 0.0f) return false;
     auto oct = [&](int st, int o, float* v) {  // state st's octave o (st is also its Y-table index)
-        octave3f<Y0, N>(s.perm + st * PERM_BYTES, ax_x(s, st, kx), ax_z(s, st, kz), s.yf[st],
-                        static_cast<float>(1 << o), v, true);
+        octave3f_y<6>(s.perm + st * PERM_BYTES, ax_x(s, st, kx), ax_z(s, st, kz), s.yf[st], y0,
+                      static_cast<float>(1 << o), v);
     };
-    return progressive_signs<N>(Y0, N, Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
+    return progressive_signs<6>(y0, n, Fe{shape[0], shape[1]}, Fe{shape[2], shape[3]}, oct, bits);
 }
 
 // CT threads per CTA, MINB CTAs per SM: chosen by the autotuner.
@@ -249,9 +252,7 @@ __global__ void __launch_bounds__(CT, MINB) k_coarse_signs_fast(StateCache cache
             unsigned bits = 0;
             bool ok;
             if (forceExact) ok = false;
-            else if (r == 0) ok = screened_range<0, 6>(s, kx, kz, s.shape[c], bits);
-            else if (r == 1) ok = screened_range<6, 6>(s, kx, kz, s.shape[c], bits);
-            else ok = screened_range<12, TOP_SOLID_LEVEL - 11>(s, kx, kz, s.shape[c], bits);  // 16 is air
+            else ok = screened_range(s, kx, kz, s.shape[c], r * 6, r == 2 ? TOP_SOLID_LEVEL - 11 : 6, bits);  // 16 is air
             if (ok) {
                 if (bits) atomicOr(&s.mask[c], bits);
                 return -1;

@@ -148,6 +148,36 @@ __device__ __forceinline__ void octave3f(const std::uint8_t* p, const AxisF& ax,
     }
 }
 
+// octave3f with the first level y0 at run time (one instantiation serves every level
+// range of a kernel, which keeps its loop code in the instruction cache). Levels
+// past 16 are clamped to 16: their values are computed but never read.
+template <int N>
+__device__ __forceinline__ void octave3f_y(const std::uint8_t* p, const AxisF& ax, const AxisF& az, const YF* yt,
+                                           int y0, float w, float* acc) {
+    const int xp0 = P(p, ax.i);
+    const int xp1 = P(p, ax.i + 1);
+    int active = -1;
+    float c00 = 0.f, c01 = 0.f, c10 = 0.f, c11 = 0.f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        const YF e = yt[min(y0 + k, 16)];
+        if (e.cell != active) {
+            active = e.cell;
+            const int p0 = xp0 + e.yi;
+            const int p00 = P(p, p0) + az.i;
+            const int p01 = P(p, p0 + 1) + az.i;
+            const int p1 = xp1 + e.yi;
+            const int p10 = P(p, p1) + az.i;
+            const int p11 = P(p, p1 + 1) + az.i;
+            c00 = lerpf(ax.fd, grad3f(P(p, p00), ax.f, e.cf, az.f), grad3f(P(p, p10), ax.f1, e.cf, az.f));
+            c01 = lerpf(ax.fd, grad3f(P(p, p01), ax.f, e.cf1, az.f), grad3f(P(p, p11), ax.f1, e.cf1, az.f));
+            c10 = lerpf(ax.fd, grad3f(P(p, p00 + 1), ax.f, e.cf, az.f1), grad3f(P(p, p10 + 1), ax.f1, e.cf, az.f1));
+            c11 = lerpf(ax.fd, grad3f(P(p, p01 + 1), ax.f, e.cf1, az.f1), grad3f(P(p, p11 + 1), ax.f1, e.cf1, az.f1));
+        }
+        acc[k] = lerpf(az.fd, lerpf(e.fd, c00, c01), lerpf(e.fd, c10, c11)) * w;
+    }
+}
+
 // FP32 2D octave value (legacy 2D sampler, NoiseGeneratorPerlin173.java:188-223).
 __device__ __forceinline__ float octave2f(const std::uint8_t* p, const AxisF& ax, const AxisF& az) {
     const int a0 = P(p, ax.i);
