@@ -55,7 +55,12 @@ struct alignas(16) WorldSmem {
     float axf[NOCT][2][NAX];   // FP32 fraction; after Lower, the 8 x 256 highest re-entry bytes
     float axd[NOCT][2][NAX];   // FP32 fade
     std::uint8_t axi[NOCT][2][NAX];  // lattice index & 255
-    std::uint32_t mask17[8][256];
+    // 17-level sign masks of the world's distinct lattice columns: centre c's column
+    // (ix, iz) is lattice column (ix + cx(c) + 15, iz + cz(c) + 15) of a 46 x 46 grid,
+    // so the columns that adjacent centres share are computed once
+    std::uint32_t maskL[NAX * NAX];
+    std::uint32_t claimed[(NAX * NAX + 31) / 32];       // lattice columns with a P20 / Upper task
+    std::uint32_t lowerClaimed[(NAX * NAX + 31) / 32];  // lattice columns with a Lower task
     float4 clim[10];  // climate generators' offsets as float pairs (climate_split)
     int p20[8], upper[8], high[8], gate[8];
 };
@@ -66,7 +71,9 @@ constexpr int SHAPE_CAP = 1536;
 
 struct FastSmem {
     WorldSmem w[PAIR];
-    std::uint16_t tasks[PAIR * 8 * 256];  // Upper: (slot << 3 | centre); Lower: (slot << 11 | centre << 8 | column)
+    std::uint16_t tasks[PAIR * 8 * 256];  // lattice-column tasks (slot << 12 | lattice index)
+    std::uint8_t units[PAIR * 8];         // centres through the P20 gate (slot << 3 | centre)
+    int unitCount;
     float4 shape[SHAPE_CAP];              // d5, its bound, d7, its bound (d5 bound < 0: undecided)
     std::uint16_t climate[SHAPE_CAP];     // wave tasks whose d5 needs the climate and noise4
     int taskCount, screened, fallbacks, climateCount;
@@ -74,6 +81,8 @@ struct FastSmem {
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
               "uint4 copies into perm and out of axf need 16-byte alignment");
+static_assert(sizeof(FastSmem) <= 227 * 1024, "one CTA's shared memory");
+static_assert(PAIR * NAX * NAX < (1 << 13) && NAX * NAX < (1 << 12), "task and fallback encodings");
 
 __device__ __forceinline__ GenTable gtab(const WorldSmem& s) {
     GenTable t;
@@ -96,13 +105,28 @@ __device__ __forceinline__ AxisF axis_of(const WorldSmem& s, int o, int a, int k
     return AxisF{f, f - 1.0f, s.axd[o][a][k], s.axi[o][a][k]};
 }
 
-__device__ __forceinline__ void column_coords(int c, int col, int& cx, int& cz, int& kx, int& kz) {
-    const int ix = col >> 4, iz = col & 15;
-    cx = -28 + ix * 4 + center_chunk_x(c) * 4;
-    cz = -28 + iz * 4 + center_chunk_z(c) * 4;
-    kx = ix + center_chunk_x(c) + 15;
-    kz = iz + center_chunk_z(c) + 15;
+// Lattice index of centre c's column col (ix = col >> 4, iz = col & 15).
+__device__ __forceinline__ int lattice_index(int c, int col) {
+    return ((col >> 4) + center_chunk_x(c) + 15) * NAX + (col & 15) + center_chunk_z(c) + 15;
 }
+
+// Coarse coordinates and axis-table indices of lattice column L (the same for
+// every centre that reads it: cx = -28 + 4 ix + 4 cx(c) = 4 kx - 88).
+__device__ __forceinline__ void lattice_coords(int L, int& cx, int& cz, int& kx, int& kz) {
+    kx = L / NAX;
+    kz = L % NAX;
+    cx = 4 * kx - 88;
+    cz = 4 * kz - 88;
+}
+
+// Claims lattice column L in a bitmap; true for the first claimant.
+__device__ __forceinline__ bool claim(std::uint32_t* bits, int L) {
+    const std::uint32_t m = 1u << (L & 31);
+    return (atomicOr(&bits[L >> 5], m) & m) == 0u;
+}
+
+constexpr std::uint32_t UPPER_BITS = 0x1F800u;  // levels 11..16
+
 
 // ---- screened FP32 path ---------------------------------------------------
 // Column shape (BetaTerrain173.java:739-804) in two passes. The first takes
@@ -111,9 +135,9 @@ __device__ __forceinline__ void column_coords(int c, int col, int& cx, int& cz, 
 // the climate and noise4 are, so only the other columns go on to the second
 // pass, which the CTA's threads share densely: the climate's ten simplex
 // octaves are the most expensive part of a screened column.
-__device__ __noinline__ bool shape_first(const WorldSmem& s, int c, int col, float4& sh) {
+__device__ __noinline__ bool shape_first(const WorldSmem& s, int L, float4& sh) {
     int cx, cz, kx, kz;
-    column_coords(c, col, cx, cz, kx, kz);
+    lattice_coords(L, cx, cz, kx, kz);
     float n5 = 0.0f;
 #pragma unroll 1
     for (int o = 0; o < 16; ++o) {
@@ -132,9 +156,9 @@ __device__ __noinline__ bool shape_first(const WorldSmem& s, int c, int col, flo
 }
 
 // Second pass: the climate and noise4 part of d5 (shape_d5_f).
-__device__ __noinline__ void shape_climate(const WorldSmem& s, int c, int col, float4& sh) {
+__device__ __noinline__ void shape_climate(const WorldSmem& s, int L, float4& sh) {
     int cx, cz, kx, kz;
-    column_coords(c, col, cx, cz, kx, kz);
+    lattice_coords(L, cx, cz, kx, kz);
     Fe temp, rain;
     climate_f(gtab(s), s.clim, cx * 4 + 2, cz * 4 + 2, temp, rain);
     float n4 = 0.0f;
@@ -153,9 +177,9 @@ __device__ __noinline__ void shape_climate(const WorldSmem& s, int c, int col, f
 // when undecided. The levels are compile-time: the top fade and the level bits
 // fold into the hot loop.
 template <int Y0, int N>
-__device__ __noinline__ bool screened_range(const WorldSmem& s, int c, int col, Fe d5, Fe d7, unsigned& bits) {
+__device__ __noinline__ bool screened_range(const WorldSmem& s, int L, Fe d5, Fe d7, unsigned& bits) {
     int cx, cz, kx, kz;
-    column_coords(c, col, cx, cz, kx, kz);
+    lattice_coords(L, cx, cz, kx, kz);
     auto oct = [&](int st, int o, float* v) {  // state st's octave o (st is also its Y-table index)
         octave3f<Y0, N>(s.perm + st * PERM_BYTES, axis_of(s, st, 0, kx), axis_of(s, st, 1, kz), s.yf[st],
                         static_cast<float>(1 << o), v, true);
@@ -171,52 +195,52 @@ __device__ __forceinline__ void range_levels(int r, int& y0, int& n) {
 }
 
 // Column ranges a task's screen left undecided, for the exact path: up to two
-// entries (range << 13 | slot << 11 | centre << 8 | column), NONE when unused.
+// entries (range << 14 | slot << 13 | lattice index), NONE when unused.
 constexpr std::uint32_t NONE = 0xFFFFFFFFu;
 struct Pending {
     std::uint32_t e[2] = {NONE, NONE};
 };
-__device__ __forceinline__ std::uint32_t fallback_entry(FastSmem& s, int q, int c, int col, int r) {
+__device__ __forceinline__ std::uint32_t fallback_entry(FastSmem& s, int q, int L, int r) {
     atomicAdd(&s.fallbacks, 1);
-    return static_cast<std::uint32_t>((r << 13) | (q << 11) | (c << 8) | col);
+    return static_cast<std::uint32_t>((r << 14) | (q << 13) | L);
 }
 
 // P20 / Upper column task of world slot q: levels 11..15 (16 is air).
-__device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int c, int col, const float4& sh, bool forceExact) {
+__device__ __forceinline__ Pending upper_task(FastSmem& s, int q, int L, const float4& sh, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 1);
     unsigned bits = 0;
     Pending p;
     if (!forceExact && sh.y >= 0.0f &&
-        screened_range<11, TOP_SOLID_LEVEL - 10>(w, c, col, Fe{sh.x, sh.y}, Fe{sh.z, sh.w}, bits)) {
-        w.mask17[c][col] = bits;
+        screened_range<11, TOP_SOLID_LEVEL - 10>(w, L, Fe{sh.x, sh.y}, Fe{sh.z, sh.w}, bits)) {
+        w.maskL[L] = bits;
         return p;
     }
-    p.e[0] = fallback_entry(s, q, c, col, 0);
+    p.e[0] = fallback_entry(s, q, L, 0);
     return p;
 }
 
 // Lower column task: levels 0..5 and 6..10 (two screened tasks) on one shape.
-__device__ __forceinline__ Pending lower_task(FastSmem& s, int q, int c, int col, const float4& sh, bool forceExact) {
+__device__ __forceinline__ Pending lower_task(FastSmem& s, int q, int L, const float4& sh, bool forceExact) {
     WorldSmem& w = s.w[q];
     atomicAdd(&s.screened, 2);
     const bool shaped = !forceExact && sh.y >= 0.0f;
     const Fe d5{sh.x, sh.y}, d7{sh.z, sh.w};
     unsigned lo = 0, hi = 0;
-    const bool okLo = shaped && screened_range<0, 6>(w, c, col, d5, d7, lo);
-    const bool okHi = shaped && screened_range<6, 5>(w, c, col, d5, d7, hi);
+    const bool okLo = shaped && screened_range<0, 6>(w, L, d5, d7, lo);
+    const bool okHi = shaped && screened_range<6, 5>(w, L, d5, d7, hi);
     const unsigned bits = (okLo ? lo : 0u) | (okHi ? hi : 0u);
-    if (bits) atomicOr(&w.mask17[c][col], bits);
+    if (bits) atomicOr(&w.maskL[L], bits);
     Pending p;
-    if (!okLo) p.e[0] = fallback_entry(s, q, c, col, 1);
-    if (!okHi) p.e[1] = fallback_entry(s, q, c, col, 2);
+    if (!okLo) p.e[0] = fallback_entry(s, q, L, 1);
+    if (!okHi) p.e[1] = fallback_entry(s, q, L, 2);
     return p;
 }
 
 // Exact FP64 column task by one whole warp (bsf_exact_warp.cuh).
-__device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int c, int col, int r) {
+__device__ __noinline__ unsigned exact_task_w(const WorldSmem& s, int L, int r) {
     int cx, cz, kx, kz;
-    column_coords(c, col, cx, cz, kx, kz);
+    lattice_coords(L, cx, cz, kx, kz);
     int y0, n;
     range_levels(r, y0, n);
     return exactwarp::exact_column_warp(s, cx, cz, y0, n);
@@ -245,9 +269,9 @@ __device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body)
                 const int src = __ffs(todo) - 1;
                 todo &= todo - 1;
                 const std::uint32_t e = __shfl_sync(0xffffffffu, p.e[i], src);
-                const int r = e >> 13, q = (e >> 11) & 1, c = (e >> 8) & 7, col = e & 255;
-                const unsigned bits = exact_task_w(s.w[q], c, col, r);
-                if (lane == 0) atomicOr(&s.w[q].mask17[c][col], bits);
+                const int r = e >> 14, q = (e >> 13) & 1, L = e & 8191;
+                const unsigned bits = exact_task_w(s.w[q], L, r);
+                if (lane == 0) atomicOr(&s.w[q].maskL[L], bits);
             }
         }
     }
@@ -257,7 +281,7 @@ __device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body)
 // Shapes of wave tasks [t0, t0 + n), n <= SHAPE_CAP, into s.shape[0, n): the
 // first pass over every task, the climate pass over the compacted list of tasks
 // that need it, each spread over all threads; a barrier after each. coord(t)
-// gives a task's (slot, centre, column). Resets the phase's task cursor k.
+// gives a task's (slot, lattice index). Resets the phase's task cursor k.
 template <int FT, typename C>
 __device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bool forceExact, C coord) {
     const int tid = threadIdx.x, lane = tid & 31;
@@ -267,9 +291,9 @@ __device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bo
             const int i = base + tid;
             bool need = false;
             if (i < n) {
-                int q, c, col;
-                coord(t0 + i, q, c, col);
-                need = shape_first(s.w[q], c, col, s.shape[i]);
+                int q, L;
+                coord(t0 + i, q, L);
+                need = shape_first(s.w[q], L, s.shape[i]);
             }
             const unsigned vote = __ballot_sync(0xffffffffu, need);
             int slot = 0;
@@ -282,9 +306,9 @@ __device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bo
     const int m = s.climateCount;
     for (int j = tid; j < m; j += FT) {
         const int i = s.climate[j];
-        int q, c, col;
-        coord(t0 + i, q, c, col);
-        shape_climate(s.w[q], c, col, s.shape[i]);
+        int q, L;
+        coord(t0 + i, q, L);
+        shape_climate(s.w[q], L, s.shape[i]);
     }
     __syncthreads();
     if (tid == 0) s.climateCount = 0;
@@ -345,7 +369,12 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
             s.taskCount = 0;
             s.cursor[0] = s.cursor[1] = s.cursor[2] = 0;
         }
-        for (int k = tid; k < nw * 8 * 256; k += FT) (&s.w[k >> 11].mask17[0][0])[k & 2047] = 0;
+        constexpr int LCOLS = NAX * NAX, LWORDS = (NAX * NAX + 31) / 32;
+        for (int k = tid; k < nw * LCOLS; k += FT) s.w[k / LCOLS].maskL[k % LCOLS] = 0;
+        for (int k = tid; k < nw * LWORDS; k += FT) {
+            s.w[k / LWORDS].claimed[k % LWORDS] = 0;
+            s.w[k / LWORDS].lowerClaimed[k % LWORDS] = 0;
+        }
         __syncthreads();
         if (tid < OCT3 * nw) {
             const int q = tid / OCT3, o = tid % OCT3;
@@ -378,109 +407,143 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         }
         __syncthreads();
 
+        // Tasks are distinct lattice columns: a column two centres share is computed once.
+        auto taskCoord = [&](int t, int& q, int& L) {
+            const int e = s.tasks[t];
+            q = e >> 12;
+            L = e & 4095;
+        };
+        auto appendTask = [&](int q, int L) {
+            const int slot = atomicAdd(&s.taskCount, 1);
+            s.tasks[slot] = static_cast<std::uint16_t>((q << 12) | L);
+        };
         // P20: the 8x8 axis columns of every centre (gpu_p20_benchmark.cpp:335-589).
         const int p20Tasks = centers * 64;
-        auto p20Coord = [&](int t, int& q, int& c, int& col) {
+        auto p20Column = [&](int t, int& q, int& c, int& L) {
             q = t / p20Tasks;
             const int u = t % p20Tasks, k = u & 63;
             c = u >> 6;
-            col = cf_axis[k >> 3] * 16 + cf_axis[k & 7];
+            L = lattice_index(c, cf_axis[k >> 3] * 16 + cf_axis[k & 7]);
         };
-        for (int t0 = 0; t0 < nw * p20Tasks; t0 += SHAPE_CAP) {
-            const int wn = min(SHAPE_CAP, nw * p20Tasks - t0);
-            shape_wave<FT>(s, 0, t0, wn, fs.forceExact, p20Coord);
+        for (int t = tid; t < nw * p20Tasks; t += FT) {
+            int q, c, L;
+            p20Column(t, q, c, L);
+            if (claim(s.w[q].claimed, L)) appendTask(q, L);
+        }
+        __syncthreads();
+        const int p20N = s.taskCount;
+        for (int t0 = 0; t0 < p20N; t0 += SHAPE_CAP) {
+            const int wn = min(SHAPE_CAP, p20N - t0);
+            shape_wave<FT>(s, 0, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 0, wn, [&](int i) {
-                int q, c, col;
-                p20Coord(t0 + i, q, c, col);
-                return upper_task(s, q, c, col, s.shape[i], fs.forceExact);
+                int q, L;
+                taskCoord(t0 + i, q, L);
+                return upper_task(s, q, L, s.shape[i], fs.forceExact);
             });
         }
+        __syncthreads();
         for (int t = tid; t < nw * p20Tasks; t += FT) {
-            const int q = t / p20Tasks, u = t % p20Tasks;
-            const int c = u >> 6, k = u & 63;
-            if (s.w[q].mask17[c][cf_axis[k >> 3] * 16 + cf_axis[k & 7]]) atomicAdd(&s.w[q].p20[c], 1);
+            int q, c, L;
+            p20Column(t, q, c, L);
+            if (s.w[q].maskL[L]) atomicAdd(&s.w[q].p20[c], 1);
         }
         __syncthreads();
         if (tid == 0) {
-            int nt = 0;
+            int nu = 0;
             for (int q = 0; q < nw; ++q) {
                 WorldSmem& w = s.w[q];
                 for (int c = 0; c < centers; ++c) {
                     const int g = prof.p20MinCount > 1 ? (w.p20[c] >= prof.p20MinCount ? w.p20[c] : 0) : w.p20[c];
                     w.gate[c] = g;
                     w.upper[c] = g;  // fullUpperCount starts from the gated P20 count (p33_shared_y.hpp:164)
-                    if (g > 0) s.tasks[nt++] = static_cast<std::uint16_t>((q << 3) | c);
+                    if (g > 0) s.units[nu++] = static_cast<std::uint8_t>((q << 3) | c);
                 }
             }
-            s.taskCount = nt;
+            s.unitCount = nu;
+            s.taskCount = 0;
         }
         __syncthreads();
-        // Upper: the 192 remaining columns of centres whose gated P20 count is positive.
-        const int upperUnits = s.taskCount;
-        auto upperCoord = [&](int t, int& q, int& c, int& col) {
-            const int e = s.tasks[t / 192];
+        // Upper: the 192 remaining columns of centres whose gated P20 count is positive,
+        // less the lattice columns P20 already computed.
+        const int upperUnits = s.unitCount;
+        auto upperColumn = [&](int t, int& q, int& c, int& L) {
+            const int e = s.units[t / 192];
             q = e >> 3;
             c = e & 7;
-            col = cf_nonaxis_cols[t % 192];
+            L = lattice_index(c, cf_nonaxis_cols[t % 192]);
         };
-        for (int t0 = 0; t0 < upperUnits * 192; t0 += SHAPE_CAP) {
-            const int wn = min(SHAPE_CAP, upperUnits * 192 - t0);
-            shape_wave<FT>(s, 1, t0, wn, fs.forceExact, upperCoord);
+        for (int t = tid; t < upperUnits * 192; t += FT) {
+            int q, c, L;
+            upperColumn(t, q, c, L);
+            if (claim(s.w[q].claimed, L)) appendTask(q, L);
+        }
+        __syncthreads();
+        const int upperN = s.taskCount;
+        for (int t0 = 0; t0 < upperN; t0 += SHAPE_CAP) {
+            const int wn = min(SHAPE_CAP, upperN - t0);
+            shape_wave<FT>(s, 1, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 1, wn, [&](int i) {
-                int q, c, col;
-                upperCoord(t0 + i, q, c, col);
-                return upper_task(s, q, c, col, s.shape[i], fs.forceExact);
+                int q, L;
+                taskCoord(t0 + i, q, L);
+                return upper_task(s, q, L, s.shape[i], fs.forceExact);
             });
         }
         __syncthreads();
         for (int t = tid; t < upperUnits * 192; t += FT) {
-            const int e = s.tasks[t / 192];
-            if (s.w[e >> 3].mask17[e & 7][cf_nonaxis_cols[t % 192]]) atomicAdd(&s.w[e >> 3].upper[e & 7], 1);
+            int q, c, L;
+            upperColumn(t, q, c, L);
+            if (s.w[q].maskL[L]) atomicAdd(&s.w[q].upper[c], 1);
         }
         __syncthreads();
         if (tid == 0) s.taskCount = 0;
         __syncthreads();
+        // Lower: levels 0..10 of the upper-positive columns of centres through the
+        // Upper gate, in two halves (p30_compact_lower.hpp:29-239) that share the
+        // column's shape; each distinct lattice column once.
         const int allCols = centers * 256;
+        auto lowerColumn = [&](int t, int& q, int& c, int& col) {
+            q = t / allCols;
+            const int u = t % allCols;
+            c = u >> 8;
+            col = u & 255;
+        };
         for (int t = tid; t < nw * allCols; t += FT) {
-            const int q = t / allCols, u = t % allCols;
-            const int c = u >> 8, col = u & 255;
+            int q, c, col;
+            lowerColumn(t, q, c, col);
             const WorldSmem& w = s.w[q];
-            if (w.gate[c] > 0 && w.upper[c] >= prof.upperMinCount && w.mask17[c][col] != 0) {
-                const int slot = atomicAdd(&s.taskCount, 1);
-                s.tasks[slot] = static_cast<std::uint16_t>((q << 11) | (c << 8) | col);
-            }
+            const int L = lattice_index(c, col);
+            if (w.gate[c] > 0 && w.upper[c] >= prof.upperMinCount && (w.maskL[L] & UPPER_BITS) != 0 &&
+                claim(s.w[q].lowerClaimed, L))
+                appendTask(q, L);
         }
         __syncthreads();
-        // Lower: levels 0..10 of the upper-positive columns, in two halves (p30_compact_lower.hpp:29-239)
-        // that share the column's shape.
         const int lowerN = s.taskCount;
-        auto lowerCoord = [&](int t, int& q, int& c, int& col) {
-            const int e = s.tasks[t];
-            q = e >> 11;
-            c = (e >> 8) & 7;
-            col = e & 255;
-        };
         for (int t0 = 0; t0 < lowerN; t0 += SHAPE_CAP) {
             const int wn = min(SHAPE_CAP, lowerN - t0);
-            shape_wave<FT>(s, 2, t0, wn, fs.forceExact, lowerCoord);
+            shape_wave<FT>(s, 2, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 2, wn, [&](int i) {
-                int q, c, col;
-                lowerCoord(t0 + i, q, c, col);
-                return lower_task(s, q, c, col, s.shape[i], fs.forceExact);
+                int q, L;
+                taskCoord(t0 + i, q, L);
+                return lower_task(s, q, L, s.shape[i], fs.forceExact);
             });
         }
         __syncthreads();
-        // Highest re-entry per lower column; each world's axis table serves as its 8x256 byte grid now.
+        // Highest re-entry per lower column of each centre through the Upper gate; each
+        // world's axis table serves as its 8 x 256 byte grid now.
         for (int k = tid; k < nw * 8 * 256; k += FT)
             reinterpret_cast<std::uint8_t*>(&s.w[k >> 11].axf[0][0][0])[k & 2047] = 0xFF;
         __syncthreads();
-        for (int t = tid; t < s.taskCount; t += FT) {
-            const int e = s.tasks[t];
-            const int q = e >> 11, c = (e >> 8) & 7, col = e & 255;
+        for (int t = tid; t < nw * allCols; t += FT) {
+            int q, c, col;
+            lowerColumn(t, q, c, col);
             WorldSmem& w = s.w[q];
-            const int h = highest_reentry(w.mask17[c][col]);
-            reinterpret_cast<std::uint8_t*>(&w.axf[0][0][0])[c * 256 + col] = h < 0 ? 0xFF : static_cast<std::uint8_t>(h);
-            if (h >= 11) atomicAdd(&w.high[c], 1);
+            const std::uint32_t m = w.maskL[lattice_index(c, col)];
+            if (w.gate[c] > 0 && w.upper[c] >= prof.upperMinCount && (m & UPPER_BITS) != 0) {
+                const int h = highest_reentry(m);
+                reinterpret_cast<std::uint8_t*>(&w.axf[0][0][0])[c * 256 + col] =
+                    h < 0 ? 0xFF : static_cast<std::uint8_t>(h);
+                if (h >= 11) atomicAdd(&w.high[c], 1);
+            }
         }
         __syncthreads();
         // Region outcomes, one warp per (world, centre); P19 candidates go to the P19 queue with their grids.
