@@ -688,6 +688,7 @@ void stage0_sweep(BsfHandle* h, std::int64_t start, std::uint64_t count, std::in
     check(cudaStreamSynchronize(h->stream), "sweep counters");
     const int fallbacks = *reinterpret_cast<const int*>(hs + 8);
     if (hs[5] != survivors) throw std::runtime_error("sweep survivor count mismatch");
+    h->lastBatch = 0;  // the region outcomes on the device are the sweep's now, not a MEGA batch's
     *nOut = survivors;
     if (counts) {
         counts->worlds = count;
