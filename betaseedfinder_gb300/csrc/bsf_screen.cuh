@@ -576,85 +576,114 @@ __device__ __forceinline__ bool column_shape_f(Fe temp, Fe rain, Fe n4, Fe n5, F
 // up to 15 and leave bit 16 clear.
 constexpr int TOP_SOLID_LEVEL = 15;
 
-// The parts of a level's density test that do not depend on noise2/noise3
-// (BetaTerrain173.java:808-822): the shape term d9 and the noise selector
-// d12 = (n1/10 + 1)/2, kept as which of d10 (noise2, bit 0) and d11 (noise3,
-// bit 1) the density may read and, for the lerp, d12 clamped to [0, 1].
+// A level's density test (BetaTerrain173.java:808-830) as two thresholds on d8.
+// The density is T(d8 - d9), where d9 = (y - d7) * 12 / d5 (times 4 when
+// negative) depends on the column shape alone and T is the top fade: the
+// identity up to level 13, above it T(x) = x (1 - d13) - 10 d13 with
+// d13 = (float)(y - 13) / 3F, increasing, zero at x = c_y = 10 d13 / (1 - d13)
+// (5.00000022 at level 14, 20.0000018 at level 15; level 16 is air). So the
+// density is positive when d8 - d9 > c_y and negative when below, and a test
+// with bounds compares our FP32 d8 with d9 + c_y give or take a margin:
+//   - d8's own error against the reference: at most E8MAX for d10 and d11
+//     (the descending sum bound and the 1/512 scaling of |sum| <= 1.55 * 65535),
+//     so for any blend of them, plus |d11 - d10| te for the selector's bound;
+//   - d9's bound, the model terms doubled (as elsewhere in this file) plus an
+//     absolute 1e-6 for the reference's own FP64 rounding of the blend, the
+//     subtraction and T (below 1e-12 for these magnitudes);
+//   - 8u (|d9| + 420) for the FP32 roundings of the test itself (the blend,
+//     |d8| <= 199 and t |d11 - d10| <= 398; the thresholds; d8 -+ the rest
+//     term), which together stay below u (2 |d9| + 1040);
+//   - the unsummed octaves: rest / 512 on d8 (1 + 2^-10 for its own rounding),
+//     not doubled, as it is an exact bound.
+// The selector d12 = (n1/10 + 1)/2 picks d10 (noise2, sel bit 0) below 0, d11
+// (noise3, bit 1) above 1, else the lerp d10 + (d11 - d10) d12; the test keeps
+// t = d12 clamped to [0, 1] and its bound te (t = 0 or 1 and te = 0 when the
+// selection is certain).
 struct LevelTerms {
-    Fe d9, t;
+    float thrPos, thrNeg;  // d8 beyond these (with rest and blend margins) decides the sign
+    float t, te;
     unsigned sel;
 };
-__device__ __forceinline__ LevelTerms level_terms(int y, Fe d5, Fe d7, float n1) {
-    LevelTerms lt;
+constexpr float E8MAX = (E_N2_DESC + OCTAVE3_ABS_MAX * 65535.0f * U) / 512.0f;
+
+// d9 = (y - d7) * 12 / d5, times 4 when negative: the shape alone.
+__device__ __forceinline__ Fe level_d9(int y, Fe d5, Fe d7) {
+    Fe d9 = fe_div(fe_scale(fe_sub(Fe{static_cast<float>(y), 0.0f}, d7), 12.0f), d5);
+    if (d9.v < 0.0f || fabsf(d9.v) <= d9.e) d9 = Fe{d9.v < 0.0f ? d9.v * 4.0f : d9.v, d9.e * 4.0f};
+    return d9;
+}
+__device__ __forceinline__ void level_thresholds(int y, Fe d5, Fe d7, LevelTerms& lt) {
+    const Fe d9 = level_d9(y, d5, d7);
+    // nearest floats to c_14 and c_15 (errors 2.3e-7 and 1.2e-7, inside the margin)
+    const float c = y <= 13 ? 0.0f : (y == 14 ? 5.0f : (y == 15 ? 20.000002f : INFINITY));
+    const float margin = 2.0f * (d9.e + E8MAX) + 1.0e-6f + 8.0f * U * (fabsf(d9.v) + 420.0f);
+    lt.thrPos = d9.v + c + margin;
+    lt.thrNeg = d9.v + c - margin;
+    lt.t = 0.0f;
+    lt.te = 0.0f;
+    lt.sel = 3u;
+}
+// The selector from the complete noise1 sum.
+__device__ __forceinline__ void level_select(float n1, LevelTerms& lt) {
     const Fe d12 = fe_scale(fe_add(fe_div(Fe{n1, E_N1}, Fe{10.0f, 0.0f}), Fe{1.0f, 0.0f}), 0.5f);
     // below 0 only d10 is read, above 1 only d11; in between (or at a clamp
     // edge) the lerp with t clamped to [0, 1] covers both sides
     lt.sel = d12.v + d12.e < 0.0f ? 1u : (d12.v - d12.e > 1.0f ? 2u : 3u);
-    lt.t = fe_clamp_hi(fe_clamp_lo(d12, 0.0f), 1.0f);
-    Fe d9 = fe_div(fe_scale(fe_sub(Fe{static_cast<float>(y), 0.0f}, d7), 12.0f), d5);
-    if (d9.v < 0.0f || fabsf(d9.v) <= d9.e) d9 = Fe{d9.v < 0.0f ? d9.v * 4.0f : d9.v, d9.e * 4.0f};
-    lt.d9 = d9;
-    return lt;
+    lt.t = lt.sel == 1u ? 0.0f : (lt.sel == 2u ? 1.0f : fminf(fmaxf(d12.v, 0.0f), 1.0f));
+    lt.te = lt.sel == 3u ? d12.e : 0.0f;
 }
 
-// Density sign at level y from noise sums with bounds: +1 / -1 when decided, 0
-// when either sign is possible. n2 / n3 may be partial sums whose unsummed
-// octaves add at most `rest` to each (an exact bound, kept apart from the FP32
-// error model): the density is d8 - d9 with d8 a convex combination of
-// n2/512 and n3/512 (d10, d11 or their lerp with t in [0, 1]), so those
-// octaves move it by at most rest / 512 times the top fade's slope (1 - d13
-// above level 13, else 1). That term is not doubled like the model's bound.
-// Written without branches: it runs once per octave pair in the screened loops.
-__device__ __forceinline__ int density_sign_lt(int y, const LevelTerms& lt, Fe n2, Fe n3, float rest = 0.0f) {
-    const Fe d10{n2.v * (1.0f / 512.0f), n2.e / 512.0f + fabsf(n2.v) * (U / 512.0f)};
-    const Fe d11{n3.v * (1.0f / 512.0f), n3.e / 512.0f + fabsf(n3.v) * (U / 512.0f)};
-    const Fe mix = fe_add(d10, fe_mul(fe_sub(d11, d10), lt.t));
-    const Fe d8 = lt.sel == 1u ? d10 : (lt.sel == 2u ? d11 : mix);
-    Fe d = fe_sub(d8, lt.d9);
-    float slope = 1.0f;
-    if (y > 13) {
-        const float d13 = static_cast<float>(y - 13) / 3.0f;  // exact as the reference's float division
-        d = fe_add(fe_mul(d, Fe{1.0f - d13, 2.0f * U}), Fe{-10.0f * d13, 20.0f * U});
-        slope = 1.0f - d13;
-    }
-    // (1 + 2^-10) covers the FP32 rounding of the rest term itself
-    const float bound = 2.0f * d.e + 1.0e-6f + rest * (slope / 512.0f) * (1.0f + 1.0f / 1024.0f);
-    return (d.v > bound ? 1 : 0) - (d.v < -bound ? 1 : 0);
-}
+// Octave pairs the screened loops sum before noise1 at most (see progressive_signs).
+#ifndef BSF_HULL_PAIRS
+#define BSF_HULL_PAIRS 16
+#endif
+constexpr int HULL_PAIRS = BSF_HULL_PAIRS;
 
-// Screened signs of one column's levels [y0, y0+n), n <= N, with noise2 and
-// noise3 summed from the largest octave (weight 2^15) down, stopping once every
-// level's sign is certain, and skipping a sum that no open level of the
-// converged lanes reads (LevelTerms::sel). Octave o contributes at most
-// OCTAVE3_ABS_MAX * 2^o, so after octaves 15..o the unsummed rest is at most
-// OCTAVE3_ABS_MAX * (2^o - 1), which density_sign_lt carries beside the sums'
-// FP32 bounds.
-// An undecided level at the end returns false (the exact FP64 path decides).
+// Screened signs of one column's levels [y0, y0+n), n <= N. noise2 and noise3
+// are summed from the largest octave (weight 2^15) down. Octave o contributes
+// at most OCTAVE3_ABS_MAX * 2^o, so after octaves 15..o the unsummed rest is
+// at most OCTAVE3_ABS_MAX * (2^o - 1), which the sign tests carry beside the
+// sums' FP32 bounds. Three phases, each warp-uniform:
+//   0. noise2 and noise3 octave o together, each level tested at both ends of
+//      the hull of d10 and d11, which needs no noise1: d8 is d10, d11 or their
+//      lerp with d12 in [0, 1], so it lies between them (the reference's FP64
+//      lerp up to three roundings, below 2^-43 for |d8| < 512 and far inside
+//      the bound's absolute 1e-6), and the density is non-decreasing in d8
+//      (the top fade's slope 1 - d13 is >= 0), so a sign both ends share is
+//      the density's sign. Most levels of the Stage0 and coarse tasks lie far
+//      enough above or below the terrain surface to be decided here. The
+//      phase ends when the warp's levels are all decided, when a level's ends
+//      have opposite certain signs (only noise1 can decide it), or after
+//      HULL_PAIRS pairs;
+//   1. the 8 noise1 octaves (the reference's order, 0.0 + first term being
+//      exact), then the selectors and a test at the depth reached;
+//   2. the remaining octaves, skipping a sum that no open level of the
+//      converged lanes reads (LevelTerms::sel), with a test after each pair.
+// A level closed in any phase keeps its sign: a later interval may straddle 0
+// again. The warp stops once all its lanes' levels are decided; an undecided
+// level after octave 0 returns false (the exact FP64 path decides).
 // oct(state, o, v) writes octave o of generator state `state`, weight 2^o, for
 // N levels from y0 into v (a level past n costs its octave work but is never
-// read). All 40 octaves go through one loop body with one octave evaluation in
+// read). Every step goes through one loop body with one octave evaluation in
 // it: the unrolled octave code is large, and a body holding several copies
-// misses the instruction cache on every iteration.
+// misses the instruction cache on every iteration. The 16 pairs and the 8
+// noise1 octaves are 40 steps.
 template <int N, typename OctFn>
 __device__ __forceinline__ bool progressive_signs(int y0, int n, Fe d5, Fe d7, OctFn oct, unsigned& bits) {
     float a1[N], a2[N], a3[N];
     LevelTerms lt[N];
 #pragma unroll
-    for (int k = 0; k < N; ++k) a1[k] = a2[k] = a3[k] = 0.0f;  // a skipped sum is read by no open level
+    for (int k = 0; k < N; ++k) {
+        a1[k] = a2[k] = a3[k] = 0.0f;  // a skipped sum is read by no open level
+        level_thresholds(y0 + k, d5, d7, lt[k]);
+    }
     unsigned open = (1u << n) - 1u, pos = 0;
-    // steps 0..7: noise1 octaves 0..7 (the reference's order, 0.0 + first term
-    // being exact); then for o = 15..0 two steps, noise2 and noise3 octave o
+    int phase = HULL_PAIRS > 0 ? 0 : 1, o = 15, i1 = 0, pairs = 0;
+    bool third = false;
 #pragma unroll 1
     for (int j = 0; j < 40; ++j) {
-        const bool n1 = j < 8;
-        const int o = n1 ? j : 15 - ((j - 8) >> 1);
-        const bool third = !n1 && ((j - 8) & 1);
         bool run = true;
-        if (!n1) {
-            if (j == 8) {
-#pragma unroll
-                for (int k = 0; k < N; ++k) lt[k] = level_terms(y0 + k, d5, d7, a1[k]);
-            }
+        if (phase == 2) {
             unsigned need = 0;
 #pragma unroll
             for (int k = 0; k < N; ++k) need |= ((open >> k) & 1u) ? lt[k].sel : 0u;
@@ -665,27 +694,57 @@ __device__ __forceinline__ bool progressive_signs(int y0, int n, Fe d5, Fe d7, O
         }
         if (run) {  // the one octave evaluation of the loop body
             float v[N];
-            oct((n1 ? ST_N1 : (third ? ST_N3 : ST_N2)) + o, o, v);
+            const bool n1 = phase == 1;
+            oct(n1 ? ST_N1 + i1 : (third ? ST_N3 : ST_N2) + o, n1 ? i1 : o, v);
 #pragma unroll
             for (int k = 0; k < N; ++k) {
-                if (n1) a1[k] = a1[k] + v[k];
+                if (phase == 1) a1[k] = a1[k] + v[k];
                 else if (third) a3[k] = a3[k] + v[k];
                 else a2[k] = a2[k] + v[k];
             }
         }
-        if (!third) continue;
-        const float rest = OCTAVE3_ABS_MAX * static_cast<float>((1 << o) - 1);  // octaves o-1..0
+        if (phase == 1) {
+            if (++i1 < 8) continue;
+#pragma unroll
+            for (int k = 0; k < N; ++k) level_select(a1[k], lt[k]);
+            phase = 2;
+        } else {
+            if (!third) {
+                third = true;
+                continue;
+            }
+            third = false;
+            --o;
+            ++pairs;
+        }
+        // both sums now hold octaves 15..o+1
+        const float rest = OCTAVE3_ABS_MAX * static_cast<float>((1 << (o + 1)) - 1);
+        const float rs = rest * (1.0f / 512.0f) * (1.0f + 1.0f / 1024.0f);
+        const bool hull = phase == 0;
+        bool conflict = false;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            // a closed level keeps its sign: a later interval may straddle 0 again
-            const int sg = density_sign_lt(y0 + k, lt[k], Fe{a2[k], E_N2_DESC}, Fe{a3[k], E_N2_DESC}, rest);
+            const float d10 = a2[k] * (1.0f / 512.0f), d11 = a3[k] * (1.0f / 512.0f);
+            const float diff = d11 - d10;
+            const float d8 = __fmaf_rn(lt[k].t, diff, d10);
+            const float em = 2.0f * fabsf(diff) * lt[k].te;
+            // phase 0: the hull's ends; then the selected d8 with its blend bound
+            const float lo = hull ? fminf(d10, d11) : d8 - em;
+            const float hi = hull ? fmaxf(d10, d11) : d8 + em;
+            const int sg = (lo - rs > lt[k].thrPos ? 1 : 0) - (hi + rs < lt[k].thrNeg ? 1 : 0);
             const bool was = (open >> k) & 1u;
+            conflict |= hull && was && hi - rs > lt[k].thrPos && lo + rs < lt[k].thrNeg;
             pos |= (was && sg > 0) ? 1u << (y0 + k) : 0u;
             open &= sg != 0 ? ~(1u << k) : ~0u;
         }
         // The converged lanes leave together: a lane that ran ahead into its
         // next task would split the warp into two instruction streams.
         if (__all_sync(__activemask(), open == 0)) break;
+        if (phase == 0) {
+            if (o < 0 || pairs >= HULL_PAIRS || __any_sync(__activemask(), conflict)) phase = 1;
+        } else if (o < 0) {
+            break;
+        }
     }
     if (open) return false;
     bits = pos;
