@@ -76,7 +76,8 @@ struct FastSmem {
     int unitCount;
     float4 shape[SHAPE_CAP];              // d5, its bound, d7, its bound (d5 bound < 0: undecided)
     std::uint16_t climate[SHAPE_CAP];     // wave tasks whose d5 needs the climate and noise4
-    int taskCount, screened, fallbacks, climateCount;
+    std::uint16_t plain[SHAPE_CAP];       // the wave's other tasks
+    int taskCount, screened, fallbacks, climateCount, plainCount;
     int cursor[3];                        // next unclaimed task of the P20, Upper and Lower phases
 };
 static_assert(sizeof(WorldSmem) % 16 == 0 && offsetof(WorldSmem, perm) == 0 && offsetof(WorldSmem, axf) % 16 == 0,
@@ -155,8 +156,8 @@ __device__ __noinline__ bool shape_first(const WorldSmem& s, int L, float4& sh) 
     return !zeroD5;
 }
 
-// Second pass: the climate and noise4 part of d5 (shape_d5_f).
-__device__ __noinline__ void shape_climate(const WorldSmem& s, int L, float4& sh) {
+// Second pass: the climate and noise4 part of d5 (shape_d5_f), as (d5, bound).
+__device__ __noinline__ float2 shape_climate(const WorldSmem& s, int L) {
     int cx, cz, kx, kz;
     lattice_coords(L, cx, cz, kx, kz);
     Fe temp, rain;
@@ -169,8 +170,7 @@ __device__ __noinline__ void shape_climate(const WorldSmem& s, int L, float4& sh
                       static_cast<float>(1 << o);
     }
     const Fe d5 = shape_d5_f(temp, rain, Fe{n4, E_N4});
-    sh.x = d5.v;
-    sh.y = d5.e;
+    return make_float2(d5.v, d5.e);
 }
 
 // Screened signs of one column's levels [Y0, Y0+N) given its shape; false
@@ -278,12 +278,18 @@ __device__ __forceinline__ void run_phase(FastSmem& s, int k, int total, F body)
     __syncthreads();
 }
 
-// Shapes of wave tasks [t0, t0 + n), n <= SHAPE_CAP, into s.shape[0, n): the
-// first pass over every task, the climate pass over the compacted list of tasks
-// that need it, each spread over all threads; a barrier after each. coord(t)
-// gives a task's (slot, lattice index). Resets the phase's task cursor k.
+// First pass of the shapes of wave tasks [t0, t0 + n), n <= SHAPE_CAP, into
+// s.shape[0, n) (spread over all threads), and the wave's task order for
+// run_phase: first the m tasks whose d5 needs the climate and noise4
+// (s.climate), then the others (s.plain), each list compacted by ballots. The
+// climate part then runs inside the task that reads it (wave_task), on warps of
+// climate tasks only, instead of as a pass of its own between two barriers:
+// such a pass kept more than half of the CTA's threads waiting, the climate
+// being needed by about 30% of the columns. The longest tasks also start first.
+// coord(t) gives a task's (slot, lattice index). Resets the phase's task
+// cursor k; returns m.
 template <int FT, typename C>
-__device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bool forceExact, C coord) {
+__device__ __forceinline__ int shape_wave(FastSmem& s, int k, int t0, int n, bool forceExact, C coord) {
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid == 0) s.cursor[k] = 0;
     if (!forceExact) {
@@ -296,22 +302,40 @@ __device__ __forceinline__ void shape_wave(FastSmem& s, int k, int t0, int n, bo
                 need = shape_first(s.w[q], L, s.shape[i]);
             }
             const unsigned vote = __ballot_sync(0xffffffffu, need);
-            int slot = 0;
-            if (lane == 0 && vote) slot = atomicAdd(&s.climateCount, __popc(vote));
+            const unsigned rest = __ballot_sync(0xffffffffu, i < n && !need);
+            int slot = 0, slotRest = 0;
+            if (lane == 0) {
+                if (vote) slot = atomicAdd(&s.climateCount, __popc(vote));
+                if (rest) slotRest = atomicAdd(&s.plainCount, __popc(rest));
+            }
             slot = __shfl_sync(0xffffffffu, slot, 0);
-            if (need) s.climate[slot + __popc(vote & ((1u << lane) - 1u))] = static_cast<std::uint16_t>(i);
+            slotRest = __shfl_sync(0xffffffffu, slotRest, 0);
+            const unsigned below = (1u << lane) - 1u;
+            if (need) s.climate[slot + __popc(vote & below)] = static_cast<std::uint16_t>(i);
+            else if (i < n) s.plain[slotRest + __popc(rest & below)] = static_cast<std::uint16_t>(i);
         }
     }
     __syncthreads();
     const int m = s.climateCount;
-    for (int j = tid; j < m; j += FT) {
-        const int i = s.climate[j];
-        int q, L;
-        coord(t0 + i, q, L);
-        shape_climate(s.w[q], L, s.shape[i]);
+    __syncthreads();  // every thread holds m before the counts are reset for the next wave
+    if (tid == 0) s.climateCount = s.plainCount = 0;
+    return m;
+}
+
+// Task i of a wave in shape_wave's order: its (slot, lattice index) and its
+// shape, the climate part computed here for the first m.
+template <typename C>
+__device__ __forceinline__ float4 wave_task(const FastSmem& s, int i, int m, int t0, bool forceExact, C coord, int& q,
+                                            int& L) {
+    const int t = forceExact ? i : (i < m ? s.climate[i] : s.plain[i - m]);
+    coord(t0 + t, q, L);
+    float4 sh = s.shape[t];
+    if (!forceExact && i < m) {
+        const float2 d5 = shape_climate(s.w[q], L);
+        sh.x = d5.x;
+        sh.y = d5.y;
     }
-    __syncthreads();
-    if (tid == 0) s.climateCount = 0;
+    return sh;
 }
 
 __device__ __forceinline__ int highest_reentry(std::uint32_t mask) {
@@ -337,7 +361,7 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     FastSmem& s = *reinterpret_cast<FastSmem*>(smem_raw);
     const int tid = threadIdx.x;
-    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.climateCount = 0; }
+    if (tid == 0) { s.screened = 0; s.fallbacks = 0; s.climateCount = 0; s.plainCount = 0; }
     for (int pair = blockIdx.x; pair * PAIR < n; pair += gridDim.x) {
         const int w0 = pair * PAIR;
         const int nw = min(PAIR, n - w0);
@@ -434,11 +458,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int p20N = s.taskCount;
         for (int t0 = 0; t0 < p20N; t0 += SHAPE_CAP) {
             const int wn = min(SHAPE_CAP, p20N - t0);
-            shape_wave<FT>(s, 0, t0, wn, fs.forceExact, taskCoord);
+            const int m = shape_wave<FT>(s, 0, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 0, wn, [&](int i) {
                 int q, L;
-                taskCoord(t0 + i, q, L);
-                return upper_task(s, q, L, s.shape[i], fs.forceExact);
+                const float4 sh = wave_task(s, i, m, t0, fs.forceExact, taskCoord, q, L);
+                return upper_task(s, q, L, sh, fs.forceExact);
             });
         }
         __syncthreads();
@@ -481,11 +505,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int upperN = s.taskCount;
         for (int t0 = 0; t0 < upperN; t0 += SHAPE_CAP) {
             const int wn = min(SHAPE_CAP, upperN - t0);
-            shape_wave<FT>(s, 1, t0, wn, fs.forceExact, taskCoord);
+            const int m = shape_wave<FT>(s, 1, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 1, wn, [&](int i) {
                 int q, L;
-                taskCoord(t0 + i, q, L);
-                return upper_task(s, q, L, s.shape[i], fs.forceExact);
+                const float4 sh = wave_task(s, i, m, t0, fs.forceExact, taskCoord, q, L);
+                return upper_task(s, q, L, sh, fs.forceExact);
             });
         }
         __syncthreads();
@@ -520,11 +544,11 @@ __global__ void __launch_bounds__(FT, MINB) k_stage0_fast(StateCache cache, int 
         const int lowerN = s.taskCount;
         for (int t0 = 0; t0 < lowerN; t0 += SHAPE_CAP) {
             const int wn = min(SHAPE_CAP, lowerN - t0);
-            shape_wave<FT>(s, 2, t0, wn, fs.forceExact, taskCoord);
+            const int m = shape_wave<FT>(s, 2, t0, wn, fs.forceExact, taskCoord);
             run_phase(s, 2, wn, [&](int i) {
                 int q, L;
-                taskCoord(t0 + i, q, L);
-                return lower_task(s, q, L, s.shape[i], fs.forceExact);
+                const float4 sh = wave_task(s, i, m, t0, fs.forceExact, taskCoord, q, L);
+                return lower_task(s, q, L, sh, fs.forceExact);
             });
         }
         __syncthreads();
