@@ -45,10 +45,10 @@ PROFILE_IDS = {"general": 0, "mega": 1, "record60": 2, "record80": 3}
 
 # DRAM bytes per world of one k_stage0_fast launch (dram__bytes_read.sum +
 # dram__bytes_write.sum from an ncu capture of an 8,192-world MEGA batch, 640x1
-# launch shape: 183.2 MB read + 43.6 MB written, divided by the worlds): the
+# launch shape: 181.3 MB read + 24.9 MB written, divided by the worlds): the
 # per-world generator cache (21,888 B) read once, region records, P19 grids and
 # spill lines. It scales in proportion to the worlds.
-STAGE0_TRAFFIC_BYTES_PER_WORLD = 27686
+STAGE0_TRAFFIC_BYTES_PER_WORLD = 25173
 
 
 def parse():
