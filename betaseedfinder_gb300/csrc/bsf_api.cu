@@ -453,9 +453,11 @@ Island exact_once(BsfHandle* h, ExactCtx& x, int world, int ccx, int ccz, int ra
                   bool preview) {
     if (radius > x.exact.maxRadius) throw std::length_error("exact radius exceeds the provisioned max_exact_radius");
     cudaStream_t st = x.stream ? x.stream : h->stream;
-    launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, x.exact, x.dIsland, preview ? h->dPrevMin : nullptr,
-                      preview ? h->dPrevMax : nullptr, h->prevCap, false, st);
-    h->launches += 12;
+    // the plain form keeps the all-FP64 scan, as its other stages do
+    const bool screened = h->mode != BSF_MODE_PLAIN && !h->fs.forceExact;
+    h->launches += launch_exact_scan(h->cache, world, ccx, ccz, radius, ms, x.exact, x.dIsland,
+                                     preview ? h->dPrevMin : nullptr, preview ? h->dPrevMax : nullptr, h->prevCap,
+                                     screened, st);
     Island isl;
     int err = 0;
     check(cudaMemcpyAsync(&isl, x.dIsland, sizeof(Island), cudaMemcpyDeviceToHost, st), "island download");

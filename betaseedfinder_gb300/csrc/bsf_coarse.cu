@@ -88,26 +88,6 @@ __device__ __forceinline__ void lattice_task(const LatticeSmem& s, double X, dou
     }
 }
 
-__device__ __forceinline__ void noise45(const GenTable& t, double X, double Z, double& n4, double& n5) {
-    double amp = 1.0;
-    double acc = 0.0;
-    for (int o = 0; o < 10; ++o) {
-        const double sc = 1.121 * amp;
-        const double v = octave2(t(ST_N4 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n4 = acc;
-    amp = 1.0;
-    for (int o = 0; o < 16; ++o) {
-        const double sc = 200.0 * amp;
-        const double v = octave2(t(ST_N5 + o), X * sc, Z * sc) * (1.0 / amp);
-        acc = o == 0 ? 0.0 + v : acc + v;
-        amp /= 2.0;
-    }
-    n5 = acc;
-}
-
 // Runs the 4 tasks of the CTA's 64 columns (threads 0..191: 3D Y ranges,
 // 192..255: 2D noise). Column (ix, iz) of the tile sits at coarse
 // (originX + ix, originZ + iz).

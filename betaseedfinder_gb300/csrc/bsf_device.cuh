@@ -395,6 +395,28 @@ __device__ __forceinline__ void column_shape(double temperature, double rain, do
     outD7 = 17.0 / 2.0 + d6 * 4.0;
 }
 
+// noise4 (10 octaves) and noise5 (16 octaves) of lattice column (X, Z), the
+// reference's 2D octave sums (BetaTerrain173.java:731-737) in its order.
+__device__ __forceinline__ void noise45(const GenTable& t, double X, double Z, double& n4, double& n5) {
+    double amp = 1.0;
+    double acc = 0.0;
+    for (int o = 0; o < 10; ++o) {
+        const double sc = 1.121 * amp;
+        const double v = octave2(t(ST_N4 + o), X * sc, Z * sc) * (1.0 / amp);
+        acc = o == 0 ? 0.0 + v : acc + v;
+        amp /= 2.0;
+    }
+    n4 = acc;
+    amp = 1.0;
+    for (int o = 0; o < 16; ++o) {
+        const double sc = 200.0 * amp;
+        const double v = octave2(t(ST_N5 + o), X * sc, Z * sc) * (1.0 / amp);
+        acc = o == 0 ? 0.0 + v : acc + v;
+        amp /= 2.0;
+    }
+    n5 = acc;
+}
+
 // Density at lattice level y (BetaTerrain173.java:808-830), yLen = 17.
 __device__ __forceinline__ double density_at(int y, double d5, double d7, double n1, double n2, double n3) {
     double d9 = (static_cast<double>(y) - d7) * 12.0 / d5;

@@ -166,13 +166,21 @@ struct ExactScratch {
     int* compStats = nullptr;        // per-root statistics (see bsf_exact.cu)
     unsigned long long* best = nullptr;
     int* err = nullptr;
+    float* lat32 = nullptr;             // screened fill: FP32 noise1..3 per lattice column and level
+    std::uint32_t* needBits = nullptr;  // (column, level) pairs the FP64 cells read
+    int* points = nullptr;              // the same pairs packed
+    int* cellList = nullptr;            // cells the screen left to FP64 (chunk << 7 | cell)
+    int* counts = nullptr;              // listed cells, packed pairs
     int maxRadius = 0;
 };
 std::size_t exact_scratch_bytes(int maxRadius);
 void exact_scratch_carve(ExactScratch& s, void* base, int maxRadius);
-void launch_exact_scan(const StateCache& cache, int world, int centerChunkX, int centerChunkZ, int radius,
-                       const MatchSettings& ms, ExactScratch& s, Island* dIsland, int* dPreviewMinY,
-                       int* dPreviewMaxY, int previewCapacity, bool reuseLattice, cudaStream_t stream);
+// One exact scan: the stone field (screened: FP32 with the FP64 operations
+// where the screen is not certain; else all FP64), components, statistics and
+// the best island. Returns the number of kernels launched.
+int launch_exact_scan(const StateCache& cache, int world, int centerChunkX, int centerChunkZ, int radius,
+                      const MatchSettings& ms, ExactScratch& s, Island* dIsland, int* dPreviewMinY,
+                      int* dPreviewMaxY, int previewCapacity, bool screened, cudaStream_t stream);
 int exact_lattice_side(int radius);
 
 }  // namespace bsf
