@@ -34,7 +34,16 @@ __constant__ unsigned char c_axis[8] = {0, 2, 5, 7, 8, 10, 13, 15};
 __constant__ unsigned char c_nonaxis_cols[192];  // full-lattice columns outside the 8x8 P20 subset
 
 constexpr int INIT_LANES = 96;
-constexpr int TAB_STRIDE = 272;  // 16-byte aligned per-lane permutation slot
+// Bytes per lane's permutation: 65 words, an odd count, so the 32 lanes' t[i]
+// of one swap step fall in 32 different banks (a stride of 68 words put 4
+// lanes in each bank).
+constexpr int TAB_STRIDE = 260;
+
+// nextInt's remainder r % b for the non-power-of-two bounds b = 256 - i of the
+// shuffle, as r - b * umulhi64(r, M[b]) with M[b] = floor(2^64 / b) + 1: for
+// r < 2^31 the product overshoots r / b by under 2^-33, while r / b sits at
+// least 1/b <= 2^-1.6 below the next integer, so the quotient is exact.
+__constant__ unsigned long long c_div_magic[257];
 
 __device__ __forceinline__ void lane_stream(int lane, int& stream, int& pos) {
     if (lane < 74) { stream = 0; pos = lane; }
@@ -73,9 +82,9 @@ __device__ __forceinline__ double next_double(std::uint64_t& s) {
 __device__ __forceinline__ void store_state(std::uint8_t* perms, double* offs, int world, int index,
                                             const std::uint8_t* tab, double a, double b, double c) {
     uint4* dst = reinterpret_cast<uint4*>(perms + (static_cast<std::size_t>(world) * ST_COUNT + index) * PERM_BYTES);
-    const uint4* src = reinterpret_cast<const uint4*>(tab);
+    const std::uint32_t* src = reinterpret_cast<const std::uint32_t*>(tab);  // 4-byte aligned slot
 #pragma unroll
-    for (int k = 0; k < 16; ++k) dst[k] = src[k];
+    for (int k = 0; k < 16; ++k) dst[k] = make_uint4(src[4 * k], src[4 * k + 1], src[4 * k + 2], src[4 * k + 3]);
     double* o = offs + (static_cast<std::size_t>(world) * ST_COUNT + index) * 4;
     o[0] = a;
     o[1] = b;
@@ -119,16 +128,18 @@ __global__ void __launch_bounds__(INIT_LANES) k_world_init(const std::int64_t* _
         b = next_double(s) * 256.0;
         c = next_double(s) * 256.0;
         bool rejected = false;
-#pragma unroll
+        // a rolled loop: fully unrolled, the 256 steps were about 100 KB of code
+#pragma unroll 4
         for (int i = 0; i < 256; ++i) {
-            const int bound = 256 - i;
+            const int bound = 256 - i;  // warp-uniform
             s = lcg_step(s);
             const std::uint32_t r = static_cast<std::uint32_t>(s >> 17);
             int j;
             if ((bound & (bound - 1)) == 0) {
                 j = static_cast<int>((static_cast<std::uint64_t>(bound) * r) >> 31);
             } else {
-                const std::uint32_t v = r % static_cast<std::uint32_t>(bound);
+                const std::uint32_t q = static_cast<std::uint32_t>(__umul64hi(r, c_div_magic[bound]));
+                const std::uint32_t v = r - q * static_cast<std::uint32_t>(bound);
                 if (static_cast<std::int32_t>(r - v + static_cast<std::uint32_t>(bound - 1)) < 0) rejected = true;
                 j = static_cast<int>(v);
             }
@@ -749,6 +760,10 @@ void init_lcg_tables() {
         }
     }
     check(cudaMemcpyToSymbol(c_jump, j, sizeof(j)), "jump table");
+    unsigned long long magic[257] = {0};
+    for (int b = 2; b <= 256; ++b)  // floor(2^64 / b) + 1; b is no power of two where it is read
+        if (b & (b - 1)) magic[b] = ~0ULL / static_cast<unsigned long long>(b) + 1;
+    check(cudaMemcpyToSymbol(c_div_magic, magic, sizeof(magic)), "division table");
     check(cudaMemcpyToSymbol(c_p19_feature, bsf_p19_feature, sizeof(bsf_p19_feature)), "p19 table");
     check(cudaMemcpyToSymbol(c_p19_left, bsf_p19_left, sizeof(bsf_p19_left)), "p19 table");
     check(cudaMemcpyToSymbol(c_p19_right, bsf_p19_right, sizeof(bsf_p19_right)), "p19 table");
