@@ -329,7 +329,8 @@ class Worker:
                                            else profile))
 
     def set_screening(self, on=True):
-        """False: every screened column task takes the exact FP64 fallback path (verification)."""
+        """False: every screened column task takes the exact FP64 fallback path and exact scans the
+        all-FP64 fill (verification; results must not change)."""
         self._check(load().bsf_set_screening(self._h, int(bool(on))))
 
     def set_persistent(self, on=True):

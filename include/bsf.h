@@ -244,8 +244,10 @@ int bsf_screen_probe(const int64_t* seeds, uint32_t worlds, uint32_t samples_per
 int bsf_set_profile(void* h, int32_t profile);
 
 /* Verification switch for the queued form: on == 0 sends every column task of
- * the screened Stage0 and coarse kernels down their exact FP64 fallback path
- * (slow; results must not change). Default on. */
+ * the screened Stage0 and coarse kernels down their exact FP64 fallback path,
+ * and exact scans (batches, bsf_exact_scan, bsf_resolve_region, bsf_preview)
+ * through the all-FP64 fill instead of the screened one (slow; results must
+ * not change). Default on. */
 int bsf_set_screening(void* h, int32_t on);
 
 /* Grid shape of the screened Stage0 and coarse kernels. on != 0 (default):
