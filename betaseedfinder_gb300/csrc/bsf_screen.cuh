@@ -10,10 +10,19 @@
 // decisions are bit-identical to the reference by construction.
 //
 // Error model (u = 2^-24, FP32 round-to-nearest, products with FMA rounded
-// once): inputs are FP64 values rounded to FP32 (error <= u|x|). For one 3D
-// octave value (corner gradients |g| <= 2, three lerp levels, all |.| <= 2):
-// gradient 2.4e-7, x-lerp 1.32e-6, y-lerp 4.56e-6, z-lerp 1.43e-5 -> E_OCT3 =
-// 2e-5. For one 2D octave value (two lerp levels): 4.6e-6 -> E_OCT2 = 6e-6.
+// once), against the FP64 value of the same expression. Inputs: lattice
+// fractions (and fraction - 1) within e_in = u + 2^-25 + 2^-30 < 1.0e-7 of
+// the FP64 ones (rounded, the subtraction of 1 rounded, the double-float
+// axis term), fades within e_f = u + 2^-30 < 6.1e-8. A gradient is +-a +- b
+// of two inputs: e_g <= 2 e_in + 2u (|g| <= 2) = 3.2e-7. A lerp
+// fma(t, b - a, a) with t in [0, 1] is the convex blend (1 - t) a + t b of its
+// operands up to the rounding of b - a (<= 4u, times t <= 1) and of the fma
+// (<= 2u, |value| <= 2), and t's error enters times |b - a| <= 4, so each
+// level adds at most 4 e_f + 6u = 6.0e-7 to its operands' error. One 3D
+// octave value (gradients, then x, y and z lerps): 3.2e-7 + 3 * 6.0e-7 =
+// 2.12e-6 -> E_OCT3 = 3e-6. One 2D octave (two lerp levels): 1.52e-6 ->
+// E_OCT2 = 2.5e-6. (The products of two errors are below 1e-13; the FP64
+// side's own rounding below 1e-14.) bsf_screen_probe measures both on the GPU.
 // Octave sums add w_o * E plus the running-sum rounding u * 2 * sum(w).
 // Everything after the octave sums is tracked per value with (value, bound)
 // pairs (struct Fe) whose operations add the propagated and rounding terms;
@@ -27,8 +36,8 @@ namespace bsf {
 namespace screen {
 
 constexpr float U = 5.9604645e-8f;  // 2^-24
-constexpr float E_OCT3 = 2.0e-5f;
-constexpr float E_OCT2 = 6.0e-6f;
+constexpr float E_OCT3 = 3.0e-6f;
+constexpr float E_OCT2 = 2.5e-6f;
 
 // Value with an upper bound of its absolute error against the FP64 reference.
 struct Fe {
@@ -386,12 +395,9 @@ __device__ __forceinline__ bool df_floor(DF v, int& out) {
 // and fraction and the fraction's fade are taken in double-float: within 2^-32
 // of the real values, and the reference's FP64 sum is within 2^-36 of its real
 // value. Rounded to FP32, the fraction and fade then carry u|x| plus at most
-// 2^-30 (the fade's slope is below 2) against the FP64 entry. That absolute
-// term moves a 3D octave value by under 10 * 2^-30 = 1e-8 (each input enters a
-// gradient or a lerp weight with a factor of at most 4, and the lerps are
-// convex), far inside the margin between E_OCT3 (2e-5) and the 1.43e-5 of its
-// derivation, and likewise for E_OCT2 (6e-6 against 4.6e-6). false when the
-// sum is within SIMPLEX_EPS of an integer: the FP64 floor decides that entry.
+// 2^-30 (the fade's slope is below 2) against the FP64 entry: the e_in and
+// e_f of the error model above count it. false when the sum is within
+// SIMPLEX_EPS of an integer: the FP64 floor decides that entry.
 __device__ __forceinline__ bool make_axis_df(int coord, DF sc, DF off, AxisF& a) {
     const DF v = df_add(df_mul_f(static_cast<float>(coord), sc), off);
     const float n = floorf(v.h);
