@@ -824,7 +824,10 @@ struct PointSmem {
 // one thread per pair: octave3_column's operations for that one level (the
 // same lattice corners, cell corners and sample, summed over octaves in the
 // reference's order), so every value equals the FP64 lattice kernel's.
-__global__ void __launch_bounds__(256) k_points_fp64(StateCache cache, int world, int originX, int originZ, int side,
+constexpr int POINT_THREADS = 64;  // >= OCT3: the CTA builds the 40 Y axes
+constexpr int CELL_THREADS = 64;
+
+__global__ void __launch_bounds__(POINT_THREADS) k_points_fp64(StateCache cache, int world, int originX, int originZ, int side,
                                                      const int* __restrict__ points, const int* __restrict__ pointCount,
                                                      LatticeBuffers lat) {
     __shared__ __align__(16) PointSmem s;
@@ -890,7 +893,7 @@ __global__ void __launch_bounds__(256) k_points_fp64(StateCache cache, int world
 }
 
 // The listed cells of the screened fill in FP64 (see above): one thread per cell.
-__global__ void __launch_bounds__(128) k_cells_fp64(StateCache cache, int world, Dims d, LatticeBuffers lat,
+__global__ void __launch_bounds__(CELL_THREADS) k_cells_fp64(StateCache cache, int world, Dims d, LatticeBuffers lat,
                                                     const int* __restrict__ cellList, const int* __restrict__ cellCount,
                                                     std::uint8_t* __restrict__ stone) {
     __shared__ __align__(16) std::uint8_t perm[ST_COUNT * PERM_BYTES];  // the climate part is staged
@@ -1022,9 +1025,12 @@ int launch_exact_scan(const StateCache& cache, int world, int ccx, int ccz, int 
         k_pack_points<<<std::min((words + 255) / 256, 152), 256, 0, stream>>>(s.needBits, words, s.points,
                                                                               s.counts + 1);
         // grid-stride loops over the device-side counts; CTAs past them return at once
-        k_points_fp64<<<std::min(static_cast<int>((cols * 9 + 255) / 256), 152 * 2), 256, 0, stream>>>(
+        // small CTAs: a CTA's points share one SM's FP64 pipe, so they set the latency
+        static_assert(POINT_THREADS >= OCT3, "Y axes");
+        k_points_fp64<<<std::min(static_cast<int>((cols * 9 + POINT_THREADS - 1) / POINT_THREADS), 152 * 8),
+                        POINT_THREADS, 0, stream>>>(
             cache, world, job.originX, job.originZ, d.side, s.points, s.counts + 1, lat);
-        k_cells_fp64<<<std::min(d.nc * d.nc, 152 * 2), 128, 0, stream>>>(cache, world, d, lat, s.cellList, s.counts,
+        k_cells_fp64<<<std::min(d.nc * d.nc * 2, 152 * 8), CELL_THREADS, 0, stream>>>(cache, world, d, lat, s.cellList, s.counts,
                                                                           s.stone);
         check(cudaGetLastError(), "screened fill");
         launches += 5;
