@@ -715,8 +715,8 @@ def main():
 
     extras = {}
     if dist.rank == 0 and not args.skip_extras:
-        # plain stage-by-stage FP64 form on the same workload (spec comparison), timed
-        # alone; then both forms' per-region records of those batches are compared byte for byte
+        # plain stage-by-stage FP64 form on the same workload (the queued form's comparison),
+        # timed alone; then both forms' per-region records of those batches are compared byte for byte
         worker.set_mode(bsf.MODE_PLAIN)
         torch.cuda.synchronize()
         p0 = time.perf_counter()
