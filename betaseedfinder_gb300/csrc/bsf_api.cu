@@ -1034,6 +1034,7 @@ void init_device_once(int device) {
     init_lcg_tables();
     init_stage0_fast();
     init_coarse_fast();
+    init_exact_tables();
     done.push_back(device);
 }
 

@@ -19,7 +19,6 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 #include <stdexcept>
 
 namespace bsf {
@@ -938,6 +937,26 @@ std::size_t align256(std::size_t v) { return (v + 255) & ~static_cast<std::size_
 
 }  // namespace
 
+// Per device (constant memory and function attributes are per device), once,
+// before any exact scan on it.
+void init_exact_tables() {
+    check(cudaFuncSetAttribute(k_exact_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(ChunkSmem)),
+          "exact smem");
+    check(cudaFuncSetAttribute(k_lattice_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(RowSmem)),
+          "lattice smem");
+    check(cudaFuncSetAttribute(k_chunks_screen, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(ScreenChunkSmem)),
+          "screen smem");
+    float2 scales[NOCT];
+    for (int o = 0; o < NOCT; ++o) {  // octave_scale_dev(o) in the same IEEE operations
+        const double base = o < 32 ? NOISE_XZ : (o < 40 ? NOISE_XZ / 80.0 : (o < 50 ? 1.121 : 200.0));
+        const int k = o < 16 ? o : (o < 32 ? o - 16 : (o < 40 ? o - 32 : (o < 50 ? o - 40 : o - 50)));
+        const double v = base * std::ldexp(1.0, -k);
+        const float h = static_cast<float>(v);
+        scales[o] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
+    }
+    check(cudaMemcpyToSymbol(ce_octave_scale, scales, sizeof(scales)), "octave scales");
+}
+
 int exact_lattice_side(int radius) { return 8 * radius + 5; }
 
 std::size_t exact_scratch_bytes(int R) {
@@ -991,25 +1010,6 @@ int launch_exact_scan(const StateCache& cache, int world, int ccx, int ccz, int 
     LatticeBuffers lat = s.lattice;
     lat.columnsPerJob = static_cast<std::size_t>(d.side) * d.side;
     const LatticeJob job{world, (ccx - radius) * 4, (ccz - radius) * 4, d.side};
-    static std::once_flag attr;  // handles on several threads launch these kernels
-    std::call_once(attr, [] {
-        check(cudaFuncSetAttribute(k_exact_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(ChunkSmem)),
-              "exact smem");
-        check(cudaFuncSetAttribute(k_lattice_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(RowSmem)),
-              "lattice smem");
-        check(cudaFuncSetAttribute(k_chunks_screen, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   sizeof(ScreenChunkSmem)),
-              "screen smem");
-        float2 scales[NOCT];
-        for (int o = 0; o < NOCT; ++o) {  // octave_scale_dev(o) in the same IEEE operations
-            const double base = o < 32 ? NOISE_XZ : (o < 40 ? NOISE_XZ / 80.0 : (o < 50 ? 1.121 : 200.0));
-            const int k = o < 16 ? o : (o < 32 ? o - 16 : (o < 40 ? o - 32 : (o < 50 ? o - 40 : o - 50)));
-            const double v = base * std::ldexp(1.0, -k);
-            const float h = static_cast<float>(v);
-            scales[o] = make_float2(h, static_cast<float>(v - static_cast<double>(h)));
-        }
-        check(cudaMemcpyToSymbol(ce_octave_scale, scales, sizeof(scales)), "octave scales");
-    });
     int launches = 0;
     if (screened) {
         // k_lattice_fast takes a lattice row per CTA and a column per thread

@@ -182,5 +182,6 @@ int launch_exact_scan(const StateCache& cache, int world, int centerChunkX, int 
                       const MatchSettings& ms, ExactScratch& s, Island* dIsland, int* dPreviewMinY,
                       int* dPreviewMaxY, int previewCapacity, bool screened, cudaStream_t stream);
 int exact_lattice_side(int radius);
+void init_exact_tables();  // per device, before its first exact scan
 
 }  // namespace bsf
